@@ -1,0 +1,278 @@
+"""GB300 (sm_103a) implementation of the implicit-boundary-integral Helmholtz
+hot path of moorhsum/Helmholtz-3D-torrone.
+
+The compute lives in the CUDA library ``libhzgb300.so`` behind the C ABI of
+``include/helmholtz_gb300.h``; this module is a thin ctypes binding of that
+ABI.  There is no CPU fallback: every call fails loudly when the library or
+a CUDA device is missing.
+
+Arrays follow the reference's conventions: grids are (N+1)^3 float64 arrays
+indexed [i, j, k] with i = y, j = x, k = z (large3Dexample2.c:428-437);
+complex vectors are numpy complex128 here and split into real/imaginary
+parts at the boundary (the reference's density / densityimg pairs).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libhzgb300.so")
+
+HZ_OK = 0
+HZ_HOST, HZ_DEVICE = 0, 1
+PREC_F64, PREC_F32, PREC_F32_REFINED = 0, 1, 2
+BICG, BICGSTAB = 0, 1
+SINGLE_LAYER, DOUBLE_LAYER = 0, 1
+RHS_POINT_DIRICHLET, RHS_POINT_NEUMANN, RHS_MONOPOLE_NEUMANN, RHS_MONOPOLE_DIRICHLET = 0, 1, 2, 3
+
+ERRORS = {-1: "HZ_ERR_ARG", -2: "HZ_ERR_CUDA", -3: "HZ_ERR_STATE", -4: "HZ_ERR_GRID",
+          -5: "HZ_ERR_NONFINITE", -6: "HZ_ERR_BREAKDOWN", -7: "HZ_ERR_DEVICE_WAIT"}
+
+
+class HzError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
+        self.code = code
+
+
+class Params(C.Structure):
+    _fields_ = [("N", C.c_int), ("int_l", C.c_double), ("int_u", C.c_double), ("wave", C.c_double),
+                ("factor", C.c_double), ("tau_factor", C.c_double), ("dirichlet", C.c_int),
+                ("interior", C.c_int), ("weno_order", C.c_int)]
+
+    @property
+    def H(self):
+        return (self.int_u - self.int_l) / self.N
+
+    @property
+    def eps(self):
+        return self.factor * self.H
+
+
+class SolveOpts(C.Structure):
+    _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
+                ("inner_tol", C.c_double), ("max_outer", C.c_int), ("stagnation", C.c_int)]
+
+
+class SolveInfo(C.Structure):
+    _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("resid", C.c_double), ("resid_f64", C.c_double),
+                ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int)]
+
+    def as_dict(self):
+        return {f: getattr(self, f) for f, _ in self._fields_}
+
+
+_lib = None
+_dp = C.POINTER(C.c_double)
+_vp = C.c_void_p
+
+# Every symbol of include/helmholtz_gb300.h with its ctypes signature.
+SIGNATURES = {
+    "hz_last_error": ([], C.c_char_p),
+    "hz_params_default": ([C.POINTER(Params), C.c_int, C.c_double], None),
+    "hz_create": ([C.POINTER(Params), C.POINTER(C.c_void_p)], C.c_int),
+    "hz_destroy": ([_vp], None),
+    "hz_set_stream": ([_vp, _vp], C.c_int),
+    "hz_get_stream": ([_vp], _vp),
+    "hz_set_distance": ([_vp, _vp, C.c_int], C.c_int),
+    "hz_build": ([_vp, C.POINTER(C.c_int64)], C.c_int),
+    "hz_tube_size": ([_vp], C.c_int64),
+    "hz_get_grids": ([_vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_get_tube": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_matvec": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_matvec_pair": ([_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_matvec_multi": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_solve": ([_vp, C.POINTER(SolveOpts), _vp, _vp, _vp, _vp, C.c_int, C.POINTER(SolveInfo)], C.c_int),
+    "hz_solve_opts_default": ([C.POINTER(SolveOpts)], None),
+    "hz_rhs_point_source": ([_vp, _vp, C.c_int, _vp, _vp, C.c_int], C.c_int),
+    "hz_eval": ([_vp, C.c_int, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_assign_gradient": ([C.c_int, C.c_double, _vp, _vp, _vp, _vp, C.c_int, C.c_int], C.c_int),
+    "hz_assign_curvatures": ([C.c_int, C.c_double, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_dense_bicg": ([C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
+                       C.POINTER(SolveInfo)], C.c_int),
+    "hz_kernel_launches": ([], C.c_int64),
+}
+
+
+def load(path=LIB_PATH):
+    """Load libhzgb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError("libhzgb300.so is not built; run __graft_entry__.build() "
+                           "or python helmholtz_3d_torrone_gb300/_build.py")
+    L = C.CDLL(path)
+    for name, (args, res) in SIGNATURES.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def _check(rc):
+    if rc != HZ_OK:
+        raise HzError(rc, load().hz_last_error().decode())
+
+
+def _ptr(a):
+    """Address of a numpy array (host) or of a torch tensor / int (device)."""
+    if a is None:
+        return None
+    if isinstance(a, int):
+        return a
+    if hasattr(a, "data_ptr"):
+        return a.data_ptr()
+    return a.ctypes.data
+
+
+def _f64(a):
+    return np.ascontiguousarray(a, dtype=np.float64)
+
+
+def params(N, wave, int_l=-2.0, int_u=2.0, factor=2.0, tau_factor=2.0, dirichlet=0, interior=0, weno_order=5):
+    """Problem parameters; defaults are the reference's compile-time values."""
+    return Params(N, int_l, int_u, wave, factor, tau_factor, dirichlet, interior, weno_order)
+
+
+def solve_opts(method=BICG, precision=PREC_F64, tol=1e-7, maxit=2000, inner_tol=1e-5, max_outer=20,
+               stagnation=1):
+    return SolveOpts(method, precision, tol, maxit, inner_tol, max_outer, stagnation)
+
+
+def kernel_launches():
+    return int(load().hz_kernel_launches())
+
+
+class Operator:
+    """Device-resident tube operator (one per surface and wave number)."""
+
+    def __init__(self, p):
+        L = load()
+        self.p = p
+        h = C.c_void_p()
+        _check(L.hz_create(C.byref(p), C.byref(h)))
+        self.h = h
+        self.n = None
+
+    def close(self):
+        if getattr(self, "h", None):
+            load().hz_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_stream(self, stream_handle):
+        _check(load().hz_set_stream(self.h, stream_handle))
+
+    def set_distance(self, d, where=HZ_HOST):
+        if where == HZ_HOST:
+            d = _f64(d)
+            S = self.p.N + 1
+            if d.size != S ** 3:
+                raise ValueError("distance grid must have (N+1)^3 = %d values" % S ** 3)
+        _check(load().hz_set_distance(self.h, _ptr(d), where))
+
+    def build(self):
+        n = C.c_int64()
+        _check(load().hz_build(self.h, C.byref(n)))
+        self.n = n.value
+        return self.n
+
+    def grids(self):
+        S = self.p.N + 1
+        g = [np.empty((S, S, S)) for _ in range(5)]
+        _check(load().hz_get_grids(self.h, *[_ptr(a) for a in g], HZ_HOST))
+        return g
+
+    def tube(self):
+        n = self.n
+        idx = np.empty(n, dtype=np.int64)
+        xs, nrm = np.empty((n, 3)), np.empty((n, 3))
+        delta, jac, reg, w = (np.empty(n) for _ in range(4))
+        _check(load().hz_get_tube(self.h, _ptr(idx), _ptr(xs), _ptr(nrm), _ptr(delta), _ptr(jac), _ptr(reg),
+                                  _ptr(w), HZ_HOST))
+        return dict(idx=idx, xs=xs, nrm=nrm, delta=delta, jac=jac, reg=reg, w=w)
+
+    def matvec(self, v, precision=PREC_F64, adjoint=False):
+        vr, vi = _f64(v.real), _f64(v.imag)
+        qr, qi = np.empty(self.n), np.empty(self.n)
+        _check(load().hz_matvec(self.h, precision, int(adjoint), _ptr(vr), _ptr(vi), _ptr(qr), _ptr(qi), HZ_HOST))
+        return qr + 1j * qi
+
+    def matvec_pair(self, v, vt, precision=PREC_F64):
+        a = [_f64(v.real), _f64(v.imag), _f64(vt.real), _f64(vt.imag)]
+        q = [np.empty(self.n) for _ in range(4)]
+        _check(load().hz_matvec_pair(self.h, precision, *[_ptr(x) for x in a], *[_ptr(x) for x in q], HZ_HOST))
+        return q[0] + 1j * q[1], q[2] + 1j * q[3]
+
+    def matvec_multi(self, V, precision=PREC_F32):
+        V = np.atleast_2d(V)
+        nrhs = V.shape[0]
+        vr, vi = _f64(V.real), _f64(V.imag)
+        qr, qi = np.empty_like(vr), np.empty_like(vi)
+        _check(load().hz_matvec_multi(self.h, precision, nrhs, _ptr(vr), _ptr(vi), _ptr(qr), _ptr(qi), HZ_HOST))
+        return qr + 1j * qi
+
+    def solve(self, b, opts=None, **kw):
+        opts = opts if opts is not None else solve_opts(**kw)
+        br, bi = _f64(b.real), _f64(b.imag)
+        xr, xi = np.empty(self.n), np.empty(self.n)
+        info = SolveInfo()
+        rc = load().hz_solve(self.h, C.byref(opts), _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), HZ_HOST, C.byref(info))
+        _check(rc)
+        return xr + 1j * xi, info.as_dict()
+
+    def rhs_point_source(self, src, kind):
+        s = _f64(src)
+        br, bi = np.empty(self.n), np.empty(self.n)
+        _check(load().hz_rhs_point_source(self.h, _ptr(s), kind, _ptr(br), _ptr(bi), HZ_HOST))
+        return br + 1j * bi
+
+    def evaluate(self, receivers, sigma, layer):
+        rx = _f64(receivers).reshape(-1, 3)
+        m = rx.shape[0]
+        sr, si = _f64(sigma.real), _f64(sigma.imag)
+        ur, ui = np.empty(m), np.empty(m)
+        _check(load().hz_eval(self.h, layer, m, _ptr(rx), _ptr(sr), _ptr(si), _ptr(ur), _ptr(ui), HZ_HOST))
+        return ur + 1j * ui
+
+
+def assign_gradient(d, N, H, weno_order=5):
+    """Device replacement of ASSIGN_GRADIENT (distance_application3D.c:56-140)."""
+    d = _f64(d)
+    g = [np.empty_like(d) for _ in range(3)]
+    _check(load().hz_assign_gradient(N, H, _ptr(d), *[_ptr(a) for a in g], weno_order, HZ_HOST))
+    return g
+
+
+def assign_curvatures(d, N, H):
+    """Device replacement of the BothCurvs loop (large3Dexample2.c:446-455)."""
+    d = _f64(d)
+    m, g = np.empty_like(d), np.empty_like(d)
+    _check(load().hz_assign_curvatures(N, H, _ptr(d), _ptr(m), _ptr(g), HZ_HOST))
+    return m, g
+
+
+def dense_bicg(A, b, tol=1e-7, maxit=1000):
+    """Device replacement of CompBiCG (BICGSTAB.c:5-339) on a dense matrix."""
+    are, aim = _f64(A.real), _f64(A.imag)
+    br, bi = _f64(b.real), _f64(b.imag)
+    n = are.shape[0]
+    xr, xi = np.empty(n), np.empty(n)
+    info = SolveInfo()
+    _check(load().hz_dense_bicg(n, _ptr(are), _ptr(aim), _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), tol, maxit,
+                                HZ_HOST, C.byref(info)))
+    return xr + 1j * xi, info.as_dict()

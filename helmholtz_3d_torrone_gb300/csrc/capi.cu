@@ -1,0 +1,790 @@
+// capi.cu -- the extern "C" boundary (include/helmholtz_gb300.h).
+#include "hz_internal.cuh"
+#include "krylov.cuh"
+
+#include <atomic>
+#include <chrono>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+namespace hz {
+
+static thread_local char g_err[1024] = "";
+static std::atomic<long long> g_launches{0};
+
+void set_error(const char *fmt, ...)
+{
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(g_err, sizeof(g_err), fmt, ap);
+    va_end(ap);
+}
+
+void note_launch(int count) { g_launches.fetch_add(count, std::memory_order_relaxed); }
+
+int DevBuf::ensure(size_t nbytes)
+{
+    if (nbytes <= bytes && ptr) return HZ_OK;
+    release();
+    if (nbytes == 0) nbytes = 16;
+    cudaError_t e = cudaMalloc(&ptr, nbytes);
+    if (e != cudaSuccess) {
+        ptr = nullptr;
+        bytes = 0;
+        set_error("cudaMalloc(%zu bytes): %s", nbytes, cudaGetErrorString(e));
+        cudaGetLastError();
+        return HZ_ERR_CUDA;
+    }
+    bytes = nbytes;
+    return HZ_OK;
+}
+
+void DevBuf::release()
+{
+    if (ptr) cudaFree(ptr);
+    ptr = nullptr;
+    bytes = 0;
+}
+
+// evaluate.cu
+int launch_eval(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *s_re, const double *s_im,
+                int64_t m, const double *rx, double wave, double tau, int interior, int layer, double *u_re,
+                double *u_im, cudaStream_t s);
+int launch_rhs(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *src, double wave, int kind,
+               double *b_re, double *b_im, cudaStream_t s);
+size_t dense_partial_elems(int64_t n);
+int launch_dense(int64_t n, const double *are, const double *aim, const double *p_re, const double *p_im,
+                 const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
+                 double *qt_im, double *part_re, double *part_im, cudaStream_t s);
+
+SweepConst sweep_const(const hz_operator *op)
+{
+    SweepConst c;
+    c.n = op->n;
+    c.wave = op->p.wave;
+    c.tau = op->tau;
+    c.dirichlet = op->p.dirichlet;
+    c.interior = op->p.interior;
+    c.err = op->err.as<unsigned>();
+    return c;
+}
+
+Rec64 rec64(hz_operator *op)
+{
+    Rec64 r;
+    r.pos = op->pos64.as<double4_32a>();
+    r.nrm = op->nrm64.as<double4_32a>();
+    return r;
+}
+
+int check_device_error(hz_operator *op, const char *where)
+{
+    unsigned e = 0;
+    HZ_CHECK_CUDA(cudaMemcpyAsync(&e, op->err.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost, op->stream));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+    if (e & DEV_ERR_WAIT) {
+        set_error("%s: a bounded device wait gave up (error word 0x%x)", where, e);
+        return HZ_ERR_DEVICE_WAIT;
+    }
+    if (e & DEV_ERR_GRID) {
+        set_error("%s: a projected point or its interpolation cell lies outside the grid", where);
+        return HZ_ERR_GRID;
+    }
+    if (e & DEV_ERR_NONFINITE) {
+        set_error("%s: non-finite value", where);
+        return HZ_ERR_NONFINITE;
+    }
+    return HZ_OK;
+}
+
+// Matrix-free operator over the tube (FP64 or FP32 sweep).
+struct MatrixFreeOp final : LinOp {
+    hz_operator *op;
+    int precision;
+    MatrixFreeOp(hz_operator *o, int prec) : op(o), precision(prec) {}
+    int apply(int mode, const double *p_re, const double *p_im, const double *pt_re, const double *pt_im,
+              double *q_re, double *q_im, double *qt_re, double *qt_im, cudaStream_t s) override
+    {
+        const SweepConst c = sweep_const(op);
+        if (precision == HZ_PREC_F64)
+            return sweep_f64(c, rec64(op), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im,
+                             op->scratch.as<double2>(), s);
+        return sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re,
+                         qt_im, op->dens32.as<float4>(), s);
+    }
+};
+
+struct DenseOp final : LinOp {
+    int64_t n;
+    const double *are, *aim;
+    double *part_re, *part_im;
+    int apply(int mode, const double *p_re, const double *p_im, const double *pt_re, const double *pt_im,
+              double *q_re, double *q_im, double *qt_re, double *qt_im, cudaStream_t s) override
+    {
+        return launch_dense(n, are, aim, (mode & SWEEP_A) ? p_re : nullptr, p_im,
+                            (mode & SWEEP_AH) ? pt_re : nullptr, pt_im, q_re, q_im, qt_re, qt_im, part_re, part_im,
+                            s);
+    }
+};
+
+}  // namespace hz
+
+using namespace hz;
+
+// Per-operator solver state (kept out of the public struct layout).
+struct hz_solver_state {
+    Krylov outer, inner;
+    DevBuf vec;  // b, x, r, q (re/im) for refinement
+    DevBuf small;
+};
+
+namespace {
+
+hz_solver_state *solver_of(hz_operator *op) { return op->solver; }
+
+int check_params(const hz_params *p)
+{
+    if (!p) {
+        set_error("params is NULL");
+        return HZ_ERR_ARG;
+    }
+    if (p->N < 8 || p->N > 4096) {
+        set_error("N = %d out of range [8, 4096]", p->N);
+        return HZ_ERR_ARG;
+    }
+    if (!(p->int_u > p->int_l)) {
+        set_error("int_u must exceed int_l");
+        return HZ_ERR_ARG;
+    }
+    if (!(p->factor > 0) || !(p->tau_factor > 0) || !std::isfinite(p->wave)) {
+        set_error("factor, tau_factor must be positive and wave finite");
+        return HZ_ERR_ARG;
+    }
+    if (p->weno_order != 3 && p->weno_order != 5) {
+        set_error("weno_order must be 3 or 5");
+        return HZ_ERR_ARG;
+    }
+    return HZ_OK;
+}
+
+int need_built(hz_operator *op)
+{
+    if (!op) {
+        set_error("operator is NULL");
+        return HZ_ERR_ARG;
+    }
+    if (!op->built) {
+        set_error("hz_build has not been run");
+        return HZ_ERR_STATE;
+    }
+    return HZ_OK;
+}
+
+// Copy count doubles in (host or device) to a device pointer.
+int stage_in(double *dst, const double *src, size_t count, int where, cudaStream_t s)
+{
+    if (!src) {
+        set_error("input pointer is NULL");
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                                  where == HZ_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    return HZ_OK;
+}
+
+int stage_out(double *dst, const double *src, size_t count, int where, cudaStream_t s)
+{
+    if (!dst) return HZ_OK;
+    HZ_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                                  where == HZ_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    return HZ_OK;
+}
+
+int where_ok(int where)
+{
+    if (where != HZ_HOST && where != HZ_DEVICE) {
+        set_error("where must be HZ_HOST or HZ_DEVICE");
+        return HZ_ERR_ARG;
+    }
+    return HZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *hz_last_error(void) { return g_err; }
+
+int64_t hz_kernel_launches(void) { return g_launches.load(); }
+
+void hz_params_default(hz_params *p, int N, double wave)
+{
+    p->N = N;
+    p->int_l = -2.0;
+    p->int_u = 2.0;
+    p->wave = wave;
+    p->factor = 2.0;
+    p->tau_factor = 2.0;
+    p->dirichlet = 0;
+    p->interior = 0;
+    p->weno_order = 5;
+}
+
+void hz_solve_opts_default(hz_solve_opts *o)
+{
+    o->method = HZ_BICG;
+    o->precision = HZ_PREC_F64;
+    o->tol = 1e-7;  // BICGSTAB.h:12 DEFAULTACC
+    o->maxit = 2000;
+    o->inner_tol = 1e-5;
+    o->max_outer = 20;
+    o->stagnation = 1;
+}
+
+int hz_create(const hz_params *p, hz_operator **out)
+{
+    HZ_TRY(check_params(p));
+    if (!out) {
+        set_error("out is NULL");
+        return HZ_ERR_ARG;
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev == 0) {
+        set_error("no CUDA device: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return HZ_ERR_CUDA;
+    }
+    hz_operator *op = new (std::nothrow) hz_operator();
+    if (!op) {
+        set_error("out of host memory");
+        return HZ_ERR_ARG;
+    }
+    op->p = *p;
+    HZ_CHECK_CUDA(cudaGetDevice(&op->device));
+    HZ_CHECK_CUDA(cudaStreamCreateWithFlags(&op->own_stream, cudaStreamNonBlocking));
+    op->stream = op->own_stream;
+    op->H = (p->int_u - p->int_l) / p->N;  // large3Dexample2.c:174
+    op->eps = p->factor * op->H;           // :350
+    op->tau = op->H * p->tau_factor;       // :4286
+    int rc = op->err.ensure(64);
+    if (rc == HZ_OK) rc = (cudaMemsetAsync(op->err.ptr, 0, 64, op->stream) == cudaSuccess) ? HZ_OK : HZ_ERR_CUDA;
+    if (rc != HZ_OK) {
+        delete op;
+        return rc;
+    }
+    op->solver = new (std::nothrow) hz_solver_state();
+    if (!op->solver) {
+        delete op;
+        set_error("out of host memory");
+        return HZ_ERR_ARG;
+    }
+    *out = op;
+    return HZ_OK;
+}
+
+void hz_destroy(hz_operator *op)
+{
+    if (!op) return;
+    cudaSetDevice(op->device);
+    if (op->stream) cudaStreamSynchronize(op->stream);
+    delete op->solver;
+    op->solver = nullptr;
+    if (op->own_stream) cudaStreamDestroy(op->own_stream);
+    delete op;
+}
+
+int hz_set_stream(hz_operator *op, void *stream)
+{
+    if (!op) {
+        set_error("operator is NULL");
+        return HZ_ERR_ARG;
+    }
+    op->stream = stream ? static_cast<cudaStream_t>(stream) : op->own_stream;
+    return HZ_OK;
+}
+
+void *hz_get_stream(hz_operator *op) { return op ? (void *)op->stream : nullptr; }
+
+int hz_set_distance(hz_operator *op, const double *d, int where)
+{
+    if (!op) {
+        set_error("operator is NULL");
+        return HZ_ERR_ARG;
+    }
+    HZ_TRY(where_ok(where));
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    const size_t S = (size_t)op->p.N + 1, nodes = S * S * S;
+    HZ_TRY(op->d.ensure(nodes * sizeof(double)));
+    HZ_TRY(stage_in(op->d.as<double>(), d, nodes, where, op->stream));
+    op->have_distance = true;
+    op->built = false;
+    return HZ_OK;
+}
+
+int hz_build(hz_operator *op, int64_t *n_out)
+{
+    if (!op) {
+        set_error("operator is NULL");
+        return HZ_ERR_ARG;
+    }
+    if (!op->have_distance) {
+        set_error("hz_set_distance has not been called");
+        return HZ_ERR_STATE;
+    }
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    const int N = op->p.N;
+    const size_t S = (size_t)N + 1, nodes = S * S * S;
+    for (DevBuf *b : {&op->gx, &op->gy, &op->gz, &op->mc, &op->gc}) HZ_TRY(b->ensure(nodes * sizeof(double)));
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    HZ_TRY(launch_grid_stencils(N, op->H, op->d.as<double>(), op->gx.as<double>(), op->gy.as<double>(),
+                                op->gz.as<double>(), op->mc.as<double>(), op->gc.as<double>(), op->p.weno_order, s));
+    int64_t n = 0;
+    HZ_TRY(tube_build(N, op->eps, op->d.as<double>(), op->idx, n, op->scratch, s));
+    op->n = n;
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    HZ_TRY(op->xs.ensure(3 * nn * sizeof(double)));
+    HZ_TRY(op->nrm.ensure(3 * nn * sizeof(double)));
+    for (DevBuf *b : {&op->delta, &op->jac, &op->reg, &op->w}) HZ_TRY(b->ensure(nn * sizeof(double)));
+    HZ_TRY(op->pos64.ensure(nn * sizeof(double4_32a)));
+    HZ_TRY(op->nrm64.ensure(nn * sizeof(double4_32a)));
+    HZ_TRY(tube_init(op->p, op->d.as<double>(), op->gx.as<double>(), op->gy.as<double>(), op->gz.as<double>(),
+                     op->mc.as<double>(), op->gc.as<double>(), n, op->idx.as<int64_t>(), op->xs.as<double>(),
+                     op->nrm.as<double>(), op->delta.as<double>(), op->jac.as<double>(), op->reg.as<double>(),
+                     op->w.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->err.as<unsigned>(), s));
+    HZ_TRY(check_device_error(op, "hz_build"));
+    // FP32 sweep records in blocked order
+    const int64_t unit = (int64_t)kThreads32 * kTgt32;  // multiple of kTile32
+    const int64_t npad = ((n + unit - 1) / unit) * unit;
+    op->r32.npad = npad;
+    if (npad > 0) {
+        HZ_TRY(op->perm.ensure(npad * sizeof(int)));
+        HZ_TRY(op->pos32.ensure(npad * sizeof(float4)));
+        HZ_TRY(op->nrm32.ensure(npad * sizeof(float4)));
+        HZ_TRY(op->tpos32.ensure(npad * sizeof(double4_32a)));
+        HZ_TRY(op->origin32.ensure((npad / kTile32) * sizeof(double4_32a)));
+        HZ_TRY(op->dens32.ensure(npad * sizeof(float4)));
+        HZ_TRY(sweep_order(N, n, op->idx.as<int64_t>(), op->perm.as<int>(), npad, op->scratch, s));
+        HZ_TRY(build_rec32(n, npad, op->perm.as<int>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
+                           op->pos32.as<float4>(), op->nrm32.as<float4>(), op->origin32.as<double4_32a>(),
+                           op->tpos32.as<double4_32a>(), s));
+    }
+    op->r32.perm = op->perm.as<int>();
+    op->r32.pos = op->pos32.as<float4>();
+    op->r32.nrm = op->nrm32.as<float4>();
+    op->r32.origin = op->origin32.as<double4_32a>();
+    op->r32.tpos = op->tpos32.as<double4_32a>();
+    // scratch for the FP64 sweep densities (double4_32a per point) and staging
+    HZ_TRY(op->scratch.ensure(nn * sizeof(double4_32a) + 256));
+    HZ_TRY(op->io.ensure(nn * sizeof(double) * 8));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    op->built = true;
+    hz_solver_state *st = solver_of(op);
+    if (st) {
+        st->outer.invalidate_graph();
+        st->inner.invalidate_graph();
+    }
+    if (n_out) *n_out = n;
+    return HZ_OK;
+}
+
+int64_t hz_tube_size(const hz_operator *op) { return op ? op->n : -1; }
+
+int hz_get_grids(hz_operator *op, double *gx, double *gy, double *gz, double *mcurv, double *gcurv, int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    const size_t S = (size_t)op->p.N + 1, nodes = S * S * S;
+    HZ_TRY(stage_out(gx, op->gx.as<double>(), nodes, where, op->stream));
+    HZ_TRY(stage_out(gy, op->gy.as<double>(), nodes, where, op->stream));
+    HZ_TRY(stage_out(gz, op->gz.as<double>(), nodes, where, op->stream));
+    HZ_TRY(stage_out(mcurv, op->mc.as<double>(), nodes, where, op->stream));
+    HZ_TRY(stage_out(gcurv, op->gc.as<double>(), nodes, where, op->stream));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(op->stream));
+    return HZ_OK;
+}
+
+int hz_get_tube(hz_operator *op, int64_t *idx, double *xs, double *nrm, double *delta, double *jac, double *reg,
+                double *w, int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    const size_t n = (size_t)op->n;
+    cudaStream_t s = op->stream;
+    if (idx)
+        HZ_CHECK_CUDA(cudaMemcpyAsync(idx, op->idx.ptr, n * sizeof(int64_t),
+                                      where == HZ_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    HZ_TRY(stage_out(xs, op->xs.as<double>(), 3 * n, where, s));
+    HZ_TRY(stage_out(nrm, op->nrm.as<double>(), 3 * n, where, s));
+    HZ_TRY(stage_out(delta, op->delta.as<double>(), n, where, s));
+    HZ_TRY(stage_out(jac, op->jac.as<double>(), n, where, s));
+    HZ_TRY(stage_out(reg, op->reg.as<double>(), n, where, s));
+    HZ_TRY(stage_out(w, op->w.as<double>(), n, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+static int matvec_common(hz_operator *op, int precision, int mode, const double *p_re, const double *p_im,
+                         const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
+                         double *qt_im, int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    if (precision < HZ_PREC_F64 || precision > HZ_PREC_F32_REFINED) {
+        set_error("unknown precision %d", precision);
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    const size_t n = (size_t)op->n;
+    if (n == 0) return HZ_OK;
+    double *io = op->io.as<double>();
+    const double *dp_re = p_re, *dp_im = p_im, *dpt_re = pt_re, *dpt_im = pt_im;
+    double *dq_re = q_re, *dq_im = q_im, *dqt_re = qt_re, *dqt_im = qt_im;
+    if (where == HZ_HOST) {
+        if (mode & SWEEP_A) {
+            HZ_TRY(stage_in(io + 0 * n, p_re, n, where, s));
+            HZ_TRY(stage_in(io + 1 * n, p_im, n, where, s));
+            dp_re = io;
+            dp_im = io + n;
+            dq_re = io + 4 * n;
+            dq_im = io + 5 * n;
+        }
+        if (mode & SWEEP_AH) {
+            HZ_TRY(stage_in(io + 2 * n, pt_re, n, where, s));
+            HZ_TRY(stage_in(io + 3 * n, pt_im, n, where, s));
+            dpt_re = io + 2 * n;
+            dpt_im = io + 3 * n;
+            dqt_re = io + 6 * n;
+            dqt_im = io + 7 * n;
+        }
+    } else {
+        if (((mode & SWEEP_A) && (!p_re || !p_im || !q_re || !q_im)) ||
+            ((mode & SWEEP_AH) && (!pt_re || !pt_im || !qt_re || !qt_im))) {
+            set_error("matvec: NULL vector");
+            return HZ_ERR_ARG;
+        }
+    }
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    MatrixFreeOp A(op, precision == HZ_PREC_F64 ? HZ_PREC_F64 : HZ_PREC_F32);
+    HZ_TRY(A.apply(mode, dp_re, dp_im, dpt_re, dpt_im, dq_re, dq_im, dqt_re, dqt_im, s));
+    if (where == HZ_HOST) {
+        if (mode & SWEEP_A) {
+            HZ_TRY(stage_out(q_re, dq_re, n, where, s));
+            HZ_TRY(stage_out(q_im, dq_im, n, where, s));
+        }
+        if (mode & SWEEP_AH) {
+            HZ_TRY(stage_out(qt_re, dqt_re, n, where, s));
+            HZ_TRY(stage_out(qt_im, dqt_im, n, where, s));
+        }
+    }
+    return check_device_error(op, "matvec");
+}
+
+int hz_matvec(hz_operator *op, int precision, int adjoint, const double *p_re, const double *p_im, double *q_re,
+              double *q_im, int where)
+{
+    if (adjoint)
+        return matvec_common(op, precision, SWEEP_AH, nullptr, nullptr, p_re, p_im, nullptr, nullptr, q_re, q_im,
+                             where);
+    return matvec_common(op, precision, SWEEP_A, p_re, p_im, nullptr, nullptr, q_re, q_im, nullptr, nullptr, where);
+}
+
+int hz_matvec_pair(hz_operator *op, int precision, const double *p_re, const double *p_im, const double *pt_re,
+                   const double *pt_im, double *q_re, double *q_im, double *qt_re, double *qt_im, int where)
+{
+    return matvec_common(op, precision, SWEEP_PAIR, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im, where);
+}
+
+int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re, const double *p_im,
+                    double *q_re, double *q_im, int where)
+{
+    HZ_TRY(need_built(op));
+    if (nrhs < 1) {
+        set_error("nrhs must be >= 1");
+        return HZ_ERR_ARG;
+    }
+    const size_t n = (size_t)op->n;
+    for (int r = 0; r < nrhs; r++)
+        HZ_TRY(hz_matvec(op, precision, 0, p_re + r * n, p_im + r * n, q_re + r * n, q_im + r * n, where));
+    return HZ_OK;
+}
+
+int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, const double *b_im, double *x_re,
+             double *x_im, int where, hz_solve_info *info)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    hz_solve_opts o;
+    if (opts_in) o = *opts_in;
+    else hz_solve_opts_default(&o);
+    if (o.method != HZ_BICG && o.method != HZ_BICGSTAB) {
+        set_error("unknown method %d", o.method);
+        return HZ_ERR_ARG;
+    }
+    if (o.precision < HZ_PREC_F64 || o.precision > HZ_PREC_F32_REFINED || !(o.tol > 0) || o.maxit < 1) {
+        set_error("bad solve options");
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    hz_solver_state *st = solver_of(op);
+    const int64_t n = op->n;
+    hz_solve_info inf{};
+    auto t0 = std::chrono::steady_clock::now();
+    if (n == 0) {
+        if (info) *info = inf;
+        return HZ_OK;
+    }
+    HZ_TRY(st->vec.ensure((size_t)n * sizeof(double) * 8));
+    HZ_TRY(st->small.ensure(vec_partial_bytes() + 64));
+    double *b0 = st->vec.as<double>();
+    double *b1 = b0 + n, *x0 = b0 + 2 * n, *x1 = b0 + 3 * n, *r0 = b0 + 4 * n, *r1 = b0 + 5 * n, *q0 = b0 + 6 * n,
+           *q1 = b0 + 7 * n;
+    HZ_TRY(stage_in(b0, b_re, n, where, s));
+    HZ_TRY(stage_in(b1, b_im, n, where, s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    int iters = 0, status = HZ_OK;
+    double resid = 0.0;
+    if (o.precision != HZ_PREC_F32_REFINED) {
+        HZ_TRY(st->outer.reserve(n));
+        MatrixFreeOp A(op, o.precision);
+        HZ_TRY(st->outer.solve(A, o.method, b0, b1, o.tol, o.maxit, o.stagnation != 0, true, s, iters, resid, status));
+        HZ_TRY(stage_out(x_re, st->outer.re(Krylov::X), n, where, s));
+        HZ_TRY(stage_out(x_im, st->outer.im(Krylov::X), n, where, s));
+        inf.iterations = iters;
+        inf.resid = resid;
+        inf.resid_f64 = (o.precision == HZ_PREC_F64) ? resid : -1.0;
+        // two matrix products per iteration (A p and A^H pt, or two A products)
+        inf.pair_evals = 2LL * iters * n * n;
+    } else {
+        // FP64 iterative refinement around FP32 inner solves.
+        HZ_TRY(st->inner.reserve(n));
+        MatrixFreeOp A32(op, HZ_PREC_F32), A64(op, HZ_PREC_F64);
+        double *part = st->small.as<double>();
+        double *dout = part + (vec_partial_bytes() / sizeof(double));
+        double normb = 0.0, nr = 0.0;
+        HZ_TRY(vec_norm(n, b0, b1, part, dout, normb, s));
+        HZ_CHECK_CUDA(cudaMemsetAsync(x0, 0, n * sizeof(double), s));
+        HZ_CHECK_CUDA(cudaMemsetAsync(x1, 0, n * sizeof(double), s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(r0, b0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(r1, b1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        nr = normb;
+        double res = (normb > 0) ? 1.0 : 0.0;
+        int outer = 0;
+        while (normb > 0 && res >= o.tol && outer < o.max_outer) {
+            outer++;
+            // inner right-hand side r / ||r|| (into q)
+            HZ_TRY(vec_scale(n, 1.0 / nr, r0, r1, q0, q1, s));
+            int it = 0, ist = HZ_OK;
+            double ires = 0.0;
+            HZ_TRY(st->inner.solve(A32, o.method, q0, q1, o.inner_tol, o.maxit, o.stagnation != 0, true, s, it, ires,
+                                   ist));
+            iters += it;
+            if (ist != HZ_OK && ist != HZ_ERR_BREAKDOWN) {
+                status = ist;
+                break;
+            }
+            HZ_TRY(vec_axpy(n, nr, st->inner.re(Krylov::X), st->inner.im(Krylov::X), x0, x1, s));
+            // r = b - A x with the FP64 sweep
+            HZ_TRY(A64.apply(SWEEP_A, x0, x1, nullptr, nullptr, q0, q1, nullptr, nullptr, s));
+            HZ_TRY(vec_sub(n, b0, b1, q0, q1, r0, r1, s));
+            HZ_TRY(vec_norm(n, r0, r1, part, dout, nr, s));
+            const double prev = res;
+            res = nr / normb;
+            if (ist == HZ_ERR_BREAKDOWN && !(res < prev)) {
+                status = HZ_ERR_BREAKDOWN;
+                break;
+            }
+        }
+        HZ_TRY(stage_out(x_re, x0, n, where, s));
+        HZ_TRY(stage_out(x_im, x1, n, where, s));
+        inf.iterations = iters;
+        inf.outer = outer;
+        inf.resid = res;
+        inf.resid_f64 = res;
+        // inner iterations: two products each; one FP64 residual product per step
+        inf.pair_evals = 2LL * iters * n * n + (long long)outer * n * n;
+    }
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    int rc = check_device_error(op, "hz_solve");
+    inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    inf.status = (rc != HZ_OK) ? rc : status;
+    if (info) *info = inf;
+    if (rc != HZ_OK) return rc;
+    if (status != HZ_OK) {
+        set_error("solver stopped early (status %d)", status);
+        return status;
+    }
+    return HZ_OK;
+}
+
+int hz_rhs_point_source(hz_operator *op, const double *src, int kind, double *b_re, double *b_im, int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    if (!src || kind < 0 || kind > 3) {
+        set_error("bad point source arguments");
+        return HZ_ERR_ARG;
+    }
+    const size_t n = (size_t)op->n;
+    cudaStream_t s = op->stream;
+    double *io = op->io.as<double>();
+    double *dre = (where == HZ_HOST) ? io : b_re, *dim = (where == HZ_HOST) ? io + n : b_im;
+    HZ_TRY(launch_rhs(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), src, op->p.wave, kind, dre, dim, s));
+    if (where == HZ_HOST) {
+        HZ_TRY(stage_out(b_re, dre, n, where, s));
+        HZ_TRY(stage_out(b_im, dim, n, where, s));
+    }
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+int hz_eval(hz_operator *op, int layer, int64_t m, const double *rx, const double *s_re, const double *s_im,
+            double *u_re, double *u_im, int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    if (layer != HZ_SINGLE_LAYER && layer != HZ_DOUBLE_LAYER) {
+        set_error("unknown layer %d", layer);
+        return HZ_ERR_ARG;
+    }
+    if (m < 0) {
+        set_error("negative receiver count");
+        return HZ_ERR_ARG;
+    }
+    if (m == 0) return HZ_OK;
+    cudaStream_t s = op->stream;
+    const size_t n = (size_t)op->n;
+    const double *drx = rx, *dsr = s_re, *dsi = s_im;
+    double *dur = u_re, *dui = u_im;
+    DevBuf tmp;
+    if (where == HZ_HOST) {
+        HZ_TRY(tmp.ensure((3 * (size_t)m + 2 * n + 2 * (size_t)m) * sizeof(double)));
+        double *t = tmp.as<double>();
+        HZ_TRY(stage_in(t, rx, 3 * m, where, s));
+        HZ_TRY(stage_in(t + 3 * m, s_re, n, where, s));
+        HZ_TRY(stage_in(t + 3 * m + n, s_im, n, where, s));
+        drx = t;
+        dsr = t + 3 * m;
+        dsi = t + 3 * m + n;
+        dur = t + 3 * m + 2 * n;
+        dui = dur + m;
+    }
+    HZ_TRY(launch_eval(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), dsr, dsi, m, drx, op->p.wave,
+                       op->tau, op->p.interior, layer, dur, dui, s));
+    if (where == HZ_HOST) {
+        HZ_TRY(stage_out(u_re, dur, m, where, s));
+        HZ_TRY(stage_out(u_im, dui, m, where, s));
+    }
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+int hz_assign_gradient(int N, double H, const double *d, double *gx, double *gy, double *gz, int weno_order,
+                       int where)
+{
+    HZ_TRY(where_ok(where));
+    if (N < 8 || !d || !gx || !gy || !gz || (weno_order != 3 && weno_order != 5)) {
+        set_error("hz_assign_gradient: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    const size_t S = (size_t)N + 1, nodes = S * S * S;
+    cudaStream_t s = nullptr;
+    if (where == HZ_DEVICE) {
+        HZ_TRY(launch_grid_stencils(N, H, d, gx, gy, gz, nullptr, nullptr, weno_order, s));
+        HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+        return HZ_OK;
+    }
+    DevBuf buf;
+    HZ_TRY(buf.ensure(4 * nodes * sizeof(double)));
+    double *b = buf.as<double>();
+    HZ_TRY(stage_in(b, d, nodes, where, s));
+    HZ_TRY(launch_grid_stencils(N, H, b, b + nodes, b + 2 * nodes, b + 3 * nodes, nullptr, nullptr, weno_order, s));
+    HZ_TRY(stage_out(gx, b + nodes, nodes, where, s));
+    HZ_TRY(stage_out(gy, b + 2 * nodes, nodes, where, s));
+    HZ_TRY(stage_out(gz, b + 3 * nodes, nodes, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+int hz_assign_curvatures(int N, double H, const double *d, double *mcurv, double *gcurv, int where)
+{
+    HZ_TRY(where_ok(where));
+    if (N < 8 || !d || !mcurv || !gcurv) {
+        set_error("hz_assign_curvatures: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    const size_t S = (size_t)N + 1, nodes = S * S * S;
+    cudaStream_t s = nullptr;
+    if (where == HZ_DEVICE) {
+        HZ_TRY(launch_grid_stencils(N, H, d, nullptr, nullptr, nullptr, mcurv, gcurv, 5, s));
+        HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+        return HZ_OK;
+    }
+    DevBuf buf;
+    HZ_TRY(buf.ensure(3 * nodes * sizeof(double)));
+    double *b = buf.as<double>();
+    HZ_TRY(stage_in(b, d, nodes, where, s));
+    HZ_TRY(launch_grid_stencils(N, H, b, nullptr, nullptr, nullptr, b + nodes, b + 2 * nodes, 5, s));
+    HZ_TRY(stage_out(mcurv, b + nodes, nodes, where, s));
+    HZ_TRY(stage_out(gcurv, b + 2 * nodes, nodes, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+int hz_dense_bicg(int64_t n, const double *a_re, const double *a_im, const double *b_re, const double *b_im,
+                  double *x_re, double *x_im, double tol, int maxit, int where, hz_solve_info *info)
+{
+    HZ_TRY(where_ok(where));
+    if (n < 1 || !a_re || !a_im || !(tol > 0) || maxit < 1) {
+        set_error("hz_dense_bicg: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    auto t0 = std::chrono::steady_clock::now();
+    cudaStream_t s = nullptr;
+    const size_t nn = (size_t)n * (size_t)n;
+    DevBuf mat, vec, part;
+    const double *dre = a_re, *dim = a_im;
+    if (where == HZ_HOST) {
+        HZ_TRY(mat.ensure(2 * nn * sizeof(double)));
+        HZ_TRY(stage_in(mat.as<double>(), a_re, nn, where, s));
+        HZ_TRY(stage_in(mat.as<double>() + nn, a_im, nn, where, s));
+        dre = mat.as<double>();
+        dim = dre + nn;
+    }
+    HZ_TRY(vec.ensure(2 * (size_t)n * sizeof(double)));
+    HZ_TRY(stage_in(vec.as<double>(), b_re, n, where, s));
+    HZ_TRY(stage_in(vec.as<double>() + n, b_im, n, where, s));
+    HZ_TRY(part.ensure(2 * dense_partial_elems(n) * sizeof(double)));
+    DenseOp A;
+    A.n = n;
+    A.are = dre;
+    A.aim = dim;
+    A.part_re = part.as<double>();
+    A.part_im = A.part_re + dense_partial_elems(n);
+    Krylov k;
+    HZ_TRY(k.reserve(n));
+    int iters = 0, status = HZ_OK;
+    double resid = 0.0;
+    HZ_TRY(k.solve(A, HZ_BICG, vec.as<double>(), vec.as<double>() + n, tol, maxit, true, false, s, iters, resid, status));
+    HZ_TRY(stage_out(x_re, k.re(Krylov::X), n, where, s));
+    HZ_TRY(stage_out(x_im, k.im(Krylov::X), n, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    if (info) {
+        hz_solve_info inf{};
+        inf.iterations = iters;
+        inf.resid = resid;
+        inf.resid_f64 = resid;
+        inf.status = status;
+        inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        *info = inf;
+    }
+    return status;
+}
+
+}  // extern "C"

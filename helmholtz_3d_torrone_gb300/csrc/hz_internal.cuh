@@ -1,0 +1,160 @@
+// hz_internal.cuh -- shared declarations of the GB300 IBIM Helmholtz library.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cstdint>
+#include <cstddef>
+#include <vector>
+
+#include "../../include/helmholtz_gb300.h"
+
+namespace hz {
+
+// ---------------------------------------------------------------- errors
+void set_error(const char *fmt, ...);
+void note_launch(int count = 1);
+
+#define HZ_CHECK_CUDA(call)                                                                      \
+    do {                                                                                         \
+        cudaError_t e_ = (call);                                                                 \
+        if (e_ != cudaSuccess) {                                                                 \
+            ::hz::set_error("%s:%d %s: %s", __FILE__, __LINE__, #call, cudaGetErrorString(e_));  \
+            return HZ_ERR_CUDA;                                                                  \
+        }                                                                                        \
+    } while (0)
+
+#define HZ_CHECK_LAUNCH()                                                                        \
+    do {                                                                                         \
+        ::hz::note_launch();                                                                     \
+        cudaError_t e_ = cudaGetLastError();                                                     \
+        if (e_ != cudaSuccess) {                                                                 \
+            ::hz::set_error("%s:%d launch: %s", __FILE__, __LINE__, cudaGetErrorString(e_));    \
+            return HZ_ERR_CUDA;                                                                  \
+        }                                                                                        \
+    } while (0)
+
+#define HZ_TRY(expr)                                                                             \
+    do {                                                                                         \
+        int rc_ = (expr);                                                                        \
+        if (rc_ != HZ_OK) return rc_;                                                            \
+    } while (0)
+
+// Bits of the device-side error word.
+enum : unsigned {
+    DEV_ERR_GRID = 1u,      // interpolation cell outside the grid
+    DEV_ERR_NONFINITE = 2u, // non-finite value produced
+    DEV_ERR_WAIT = 4u,      // a bounded wait on an mbarrier gave up
+    DEV_ERR_NORMAL = 8u,    // interpolated gradient norm far from 1 (reference warns)
+};
+
+// Spin limit of every mbarrier wait (polls); far above any real wait.
+constexpr long long kWaitLimit = 1ll << 24;
+
+// ----------------------------------------------------------- device memory
+struct DevBuf {
+    void *ptr = nullptr;
+    size_t bytes = 0;
+    DevBuf() = default;
+    DevBuf(const DevBuf &) = delete;
+    DevBuf &operator=(const DevBuf &) = delete;
+    ~DevBuf() { release(); }
+    int ensure(size_t nbytes);  // grow-only
+    void release();
+    template <class T> T *as() const { return static_cast<T *>(ptr); }
+};
+
+// ------------------------------------------------------------ sweep types
+// Source/target record of the FP64 sweep (lexicographic tube order).
+struct Rec64 {
+    double4_32a *pos;  // x*, y*, z*, reg
+    double4_32a *nrm;  // nx, ny, nz, w
+};
+
+// Tile geometry of the FP32 sweep.
+constexpr int kTile32 = 256;  // sources per shared-memory tile
+constexpr int kThreads32 = 256;
+constexpr int kTgt32 = 2;     // targets per thread
+constexpr int kTile64 = 128;
+constexpr int kThreads64 = 128;
+
+// Sweep-order (spatially blocked) FP32 records.  perm[s] is the tube index
+// of sweep slot s; slots >= n are padding with zero weight.
+struct Rec32 {
+    int64_t npad;        // multiple of kTile32 and of kThreads32*kTgt32
+    int *perm;           // npad entries, -1 for padding
+    float4 *pos;         // x-o, y-o, z-o relative to the slot's tile origin; .w = reg
+    float4 *nrm;         // nx, ny, nz, w
+    double4_32a *origin;     // per tile: origin (x, y, z), unused
+    double4_32a *tpos;       // per slot FP64 position (x, y, z), .w = w (targets)
+};
+
+struct SweepConst {
+    int64_t n;
+    double wave;
+    double tau;
+    int dirichlet;
+    int interior;
+    unsigned *err;  // device error word
+};
+
+// sweep modes
+enum { SWEEP_A = 1, SWEEP_AH = 2, SWEEP_PAIR = 3 };
+
+// stencils.cu
+int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
+                         double *mc, double *gc, int order, cudaStream_t s);
+// tube.cu
+int tube_build(int N, double eps, const double *d, DevBuf &idx, int64_t &n, DevBuf &scratch,
+               cudaStream_t s);
+int tube_init(const hz_params &p, const double *d, const double *gx, const double *gy,
+              const double *gz, const double *mc, const double *gc, int64_t n, const int64_t *idx,
+              double *xs, double *nrm, double *delta, double *jac, double *reg, double *w,
+              double4_32a *pos64, double4_32a *nrm64, unsigned *err, cudaStream_t s);
+int sweep_order(int N, int64_t n, const int64_t *idx, int *perm, int64_t npad, DevBuf &scratch,
+                cudaStream_t s);
+int build_rec32(int64_t n, int64_t npad, const int *perm, const double4_32a *pos64,
+                const double4_32a *nrm64, float4 *pos32, float4 *nrm32, double4_32a *origin,
+                double4_32a *tpos, cudaStream_t s);
+// sweep_f64.cu
+int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re, const double *p_im,
+              const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
+              double *qt_im, double2 *scratch, cudaStream_t s);
+// sweep_f32.cu
+int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode,
+              const double *p_re, const double *p_im, const double *pt_re, const double *pt_im,
+              double *q_re, double *q_im, double *qt_re, double *qt_im, float4 *dens,
+              cudaStream_t s);
+
+}  // namespace hz
+
+struct hz_solver_state;
+
+// The operator handle.
+struct hz_operator {
+    hz_params p{};
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    cudaStream_t own_stream = nullptr;
+    double H = 0, eps = 0, tau = 0;
+    // grids
+    hz::DevBuf d, gx, gy, gz, mc, gc;
+    bool have_distance = false, built = false;
+    // tube
+    int64_t n = 0;
+    hz::DevBuf idx, xs, nrm, delta, jac, reg, w;
+    hz::DevBuf pos64, nrm64;
+    // FP32 sweep records
+    hz::Rec32 r32{};
+    hz::DevBuf perm, pos32, nrm32, origin32, tpos32;
+    // scratch and error word
+    hz::DevBuf scratch, err;
+    hz::DevBuf io;  // staging for host <-> device vectors
+    hz::DevBuf dens32;
+    hz_solver_state *solver = nullptr;  // Krylov workspaces (capi.cu)
+};
+
+namespace hz {
+int check_device_error(hz_operator *op, const char *where);
+hz::SweepConst sweep_const(const hz_operator *op);
+hz::Rec64 rec64(hz_operator *op);
+}  // namespace hz

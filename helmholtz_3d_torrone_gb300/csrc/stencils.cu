@@ -1,0 +1,249 @@
+// stencils.cu -- WENO gradient and curvature grids (FP64).
+//
+// Built with -fmad=false: every expression keeps the reference's unfused
+// operation order, so the grids are bit-identical to the reference C code
+// (weno.c:259-345, distance_application3D.c:35-140,
+// finite_difference3D.c:220-721) on the same distance grid.
+//
+// On GB300 these kernels are bound by the FP64 pipe (about 1.2 TFLOP/s,
+// roughly 1/60 of FP32), not by HBM: a node costs ~750 FP64 operations
+// (WENO weights need six IEEE divisions per axis, the cross derivatives
+// nine candidates per plane) against 48 bytes of compulsory traffic.  One
+// thread per node with read-only cached loads is therefore enough; the
+// neighbourhood is served by L1/L2.
+#include "hz_internal.cuh"
+
+namespace hz {
+namespace {
+
+__device__ __forceinline__ int mirror(int x, int N) { return x < 0 ? -x : (x > N ? 2 * N - x : x); }
+
+// tools.c:296-310: max/min with the reference's tie and signed-zero rules.
+__device__ __forceinline__ double rmax(double a, double b) { return (a >= b) ? a : b; }
+__device__ __forceinline__ double rmin(double a, double b) { return (a <= b) ? a : b; }
+
+// weno.c:259-345
+__device__ void weno(double *dfp, double *dfn, const double *fi, double dx, int order)
+{
+    double aa, bb, cc, dd, ee, ff, df, ih;
+    double IS0, IS1, IS2, a0, a1, a2, w0, w1, w2;
+    const double eps = 1e-12;
+    ih = 1. / dx;
+    if (order == 3) {
+        aa = fi[1] - fi[0];
+        bb = fi[2] - fi[1];
+        cc = fi[3] - fi[2];
+        dd = fi[4] - fi[3];
+        df = bb + cc;
+        a0 = bb - aa;
+        a1 = cc - bb;
+        a2 = dd - cc;
+        IS0 = (eps + a2 * a2) / (eps + a1 * a1);
+        w0 = 1. / (1. + 2. * IS0 * IS0);
+        *dfp = .5 * ih * (df - w0 * (dd - 2. * cc + bb));
+        IS0 = (eps + a0 * a0) / (eps + a1 * a1);
+        w0 = 1 / (1 + 2. * IS0 * IS0);
+        *dfn = .5 * ih * (df - w0 * (aa - 2. * bb + cc));
+        return;
+    }
+    aa = (fi[1] - fi[0]) * ih;
+    bb = (fi[2] - fi[1]) * ih;
+    cc = (fi[3] - fi[2]) * ih;
+    dd = (fi[4] - fi[3]) * ih;
+    ee = (fi[5] - fi[4]) * ih;
+    ff = (fi[6] - fi[5]) * ih;
+    df = (-bb + 7. * (cc + dd) - ee) / 12.;
+    aa = bb - aa;
+    bb = cc - bb;
+    cc = dd - cc;
+    dd = ee - dd;
+    ee = ff - ee;
+    IS0 = 13. * (ee - dd) * (ee - dd) + 3. * (ee - 3. * dd) * (ee - 3. * dd);
+    IS1 = 13. * (dd - cc) * (dd - cc) + 3. * (dd + cc) * (dd + cc);
+    IS2 = 13. * (cc - bb) * (cc - bb) + 3. * (3. * cc - bb) * (3. * cc - bb);
+    a0 = 1. / ((eps + IS0) * (eps + IS0));
+    a1 = 6. / ((eps + IS1) * (eps + IS1));
+    a2 = 3. / ((eps + IS2) * (eps + IS2));
+    w1 = 1. / (a0 + a1 + a2);
+    w0 = a0 * w1;
+    w2 = a2 * w1;
+    *dfp = df + w0 * (ee - 2. * dd + cc) / 3. + (w2 - .5) * (dd - 2. * cc + bb) / 6.;
+    IS0 = 13. * (aa - bb) * (aa - bb) + 3. * (aa - 3. * bb) * (aa - 3. * bb);
+    IS1 = 13. * (bb - cc) * (bb - cc) + 3. * (bb + cc) * (bb + cc);
+    IS2 = 13. * (cc - dd) * (cc - dd) + 3. * (3. * cc - dd) * (3. * cc - dd);
+    a0 = 1. / ((eps + IS0) * (eps + IS0));
+    a1 = 6. / ((eps + IS1) * (eps + IS1));
+    a2 = 3. / ((eps + IS2) * (eps + IS2));
+    w1 = 1. / (a0 + a1 + a2);
+    w0 = a0 * w1;
+    w2 = a2 * w1;
+    *dfn = df - w0 * (aa - 2. * bb + cc) / 3. - (w2 - .5) * (bb - 2. * cc + dd) / 6.;
+}
+
+// Values along one axis through the node: v(m) = d[base + m*stride].
+struct Line {
+    const double *__restrict__ d;
+    long long base, stride;
+    __device__ double operator()(int m) const { return __ldg(d + base + (long long)m * stride); }
+};
+
+// finite_difference3D.c:220-390; xorder selects XDER2's min_abs argument order.
+__device__ double der2(const Line &L, int c, int N, double H, bool xorder)
+{
+    double DDp, DDc, DDn;
+    if (c == 0) return 2.0 * (L(1) - L(0)) / (H * H);
+    if (c == N) return 2.0 * (L(-1) - L(0)) / (H * H);
+    if (c < 3) {
+        DDp = (2.0 * L(0) - 5.0 * L(1) + 4.0 * L(2) - L(3)) / (H * H);
+        DDc = (L(1) - 2.0 * L(0) + L(-1)) / (H * H);
+        return (fabs(DDp) < fabs(DDc)) ? DDp : DDc;
+    }
+    if (c > N - 3) {
+        DDn = (2.0 * L(0) - 5.0 * L(-1) + 4.0 * L(-2) - L(-3)) / (H * H);
+        DDc = (L(1) - 2.0 * L(0) + L(-1)) / (H * H);
+        return (fabs(DDn) < fabs(DDc)) ? DDn : DDc;
+    }
+    double Dpp = L(2) - L(1), Dp = L(1) - L(0), Dn = L(0) - L(-1), Dnn = L(-1) - L(-2);
+    DDp = (2.0 * L(0) - 5.0 * L(1) + 4.0 * L(2) - L(3)) / (H * H);
+    DDc = (L(1) - 2.0 * L(0) + L(-1)) / (H * H);
+    DDn = (2.0 * L(0) - 5.0 * L(-1) + 4.0 * L(-2) - L(-3)) / (H * H);
+    if ((Dp * Dnn <= 0.0) && (Dpp * Dn <= 0.0)) {
+        double a = DDp, b = xorder ? DDc : DDn, c3 = xorder ? DDn : DDc;
+        double q = (fabs(a) < fabs(b)) ? a : b;  // tools.c:338-343
+        return (fabs(q) < fabs(c3)) ? q : c3;
+    } else if (Dp * Dnn <= 0.0) {
+        return (fabs(DDp) < fabs(DDc)) ? DDp : DDc;
+    } else if (Dpp * Dn <= 0.0) {
+        return (fabs(DDn) < fabs(DDc)) ? DDn : DDc;
+    }
+    return DDc;
+}
+
+struct Plane {
+    const double *__restrict__ d;
+    long long base, sa, sb;
+    __device__ double operator()(int u, int v) const
+    {
+        return __ldg(d + base + (long long)u * sa + (long long)v * sb);
+    }
+};
+
+// finite_difference3D.c:393-721 (secondpartialxy/xz/yz).
+__device__ double cross(const Plane &P, int ca, int cb, int N, double H)
+{
+    const double coef[3] = {1.0, -4.0, 3.0};
+    if ((ca == 0) || (ca == N) || (cb == 0) || (cb == N)) return 0.0;
+    if ((ca < 2) || (ca > N - 2) || (cb < 2) || (cb > N - 2))
+        return (P(1, 1) - P(-1, 1) - P(1, -1) + P(-1, -1)) / (4.0 * H * H);
+    double fin = 1000000.0;  // LARGENUM
+#pragma unroll
+    for (int di = 0; di < 3; di++)
+#pragma unroll
+        for (int dj = 0; dj < 3; dj++) {
+            double v = 0.0;
+            if ((di == 1) && (dj == 1)) {
+                v = (P(1, 1) - P(-1, 1) - P(1, -1) + P(-1, -1));
+            } else if (di == 1) {
+                const int sign = dj - 1;
+#pragma unroll
+                for (int c = 2; c >= 0; c--)
+                    v += (-1.0 * (double)(sign)*coef[2 - c] * (P(1, sign * c) - P(-1, sign * c)));
+            } else if (dj == 1) {
+                const int sign = di - 1;
+#pragma unroll
+                for (int c = 2; c >= 0; c--)
+                    v += (-1.0 * (double)(sign)*coef[2 - c] * (P(sign * c, 1) - P(sign * c, -1)));
+            } else {
+                const int si = di - 1, sj = dj - 1, sij = si * sj;
+#pragma unroll
+                for (int ci = 2; ci >= 0; ci--)
+#pragma unroll
+                    for (int cj = 2; cj >= 0; cj--) {
+                        // allcoef[a][b] = coef[a]*coef[b]
+                        const double ac = coef[2 - ci] * coef[2 - cj];
+                        v += (ac * (double)(sij)*P(si * ci, sj * cj));
+                    }
+            }
+            if (fabs(v) < fabs(fin)) fin = v;
+        }
+    return fin / (4.0 * H * H);
+}
+
+__global__ void __launch_bounds__(256) grid_kernel(int N, double H, const double *__restrict__ d,
+                                                   double *__restrict__ gx, double *__restrict__ gy,
+                                                   double *__restrict__ gz, double *__restrict__ mc,
+                                                   double *__restrict__ gc, int order)
+{
+    const long long S = N + 1;
+    const long long total = S * S * S;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
+         o += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(o % S);
+        const int j = (int)((o / S) % S);
+        const int i = (int)(o / (S * S));
+        if (gx) {
+            // distance_application3D.c:56-140 with WENO_DX/DY/DZ (weno.c:117-254)
+            const int half = (order == 5) ? 3 : 2;
+            double f[7], Dxp, Dxn, Dyp, Dyn, Dzp, Dzn;
+            for (int m = -half; m <= half; m++) f[m + half] = __ldg(d + (i * S + mirror(j + m, N)) * S + k);
+            weno(&Dxp, &Dxn, f, H, order);
+            for (int m = -half; m <= half; m++) f[m + half] = __ldg(d + (mirror(i + m, N) * S + j) * S + k);
+            weno(&Dyp, &Dyn, f, H, order);
+            for (int m = -half; m <= half; m++) f[m + half] = __ldg(d + (i * S + j) * S + mirror(k + m, N));
+            weno(&Dzp, &Dzn, f, H, order);
+            const double aplus = rmax(0.0, Dxp), aminus = rmin(0.0, Dxp);
+            const double bplus = rmax(0.0, Dxn), bminus = rmin(0.0, Dxn);
+            const double cplus = rmax(0.0, Dyp), cminus = rmin(0.0, Dyp);
+            const double dplus = rmax(0.0, Dyn), dminus = rmin(0.0, Dyn);
+            const double eplus = rmax(0.0, Dzp), eminus = rmin(0.0, Dzp);
+            const double fplus = rmax(0.0, Dzn), fminus = rmin(0.0, Dzn);
+            double rx, ry, rz;
+            if (__ldg(d + o) > 0.0) {
+                rx = (fabs(aminus) > fabs(bplus)) ? aminus : bplus;
+                ry = (fabs(cminus) > fabs(dplus)) ? cminus : dplus;
+                rz = (fabs(eminus) > fabs(fplus)) ? eminus : fplus;
+            } else {
+                rx = (fabs(aplus) > fabs(bminus)) ? aplus : bminus;
+                ry = (fabs(cplus) > fabs(dminus)) ? cplus : dminus;
+                rz = (fabs(eplus) > fabs(fminus)) ? eplus : fminus;
+            }
+            gx[o] = rx;
+            gy[o] = ry;
+            gz[o] = rz;
+        }
+        if (mc) {
+            // distance_application3D.c:35-53
+            const Line Lx{d, o, S}, Ly{d, o, S * S}, Lz{d, o, 1};
+            const double dxx = der2(Lx, j, N, H, true);
+            const double dyy = der2(Ly, i, N, H, false);
+            const double dzz = der2(Lz, k, N, H, false);
+            const double dxy = cross(Plane{d, o, S * S, S}, i, j, N, H);
+            const double dxz = cross(Plane{d, o, S, 1}, j, k, N, H);
+            const double dyz = cross(Plane{d, o, S * S, 1}, i, k, N, H);
+            const double diag = dxx * dyy + dyy * dzz + dxx * dzz;
+            const double crs = dxy * dxy + dyz * dyz + dxz * dxz;
+            mc[o] = -0.5 * (dxx + dyy + dzz);
+            gc[o] = diag - crs;
+        }
+    }
+}
+
+}  // namespace
+
+int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
+                         double *mc, double *gc, int order, cudaStream_t s)
+{
+    const long long S = N + 1, total = S * S * S;
+    int sms = 152;
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long blocks = (total + 255) / 256;
+    const long long cap = (long long)sms * 16;
+    if (blocks > cap) blocks = cap;
+    grid_kernel<<<(unsigned)blocks, 256, 0, s>>>(N, H, d, gx, gy, gz, mc, gc, order);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
+}  // namespace hz

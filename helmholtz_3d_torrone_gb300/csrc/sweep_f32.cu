@@ -1,0 +1,268 @@
+// sweep_f32.cu -- FP32 matrix-free pair sweep (the bulk matvec of the
+// mixed-precision solver): the same operator as sweep_f64.cu, evaluated on
+// the FP32 and SFU pipes.
+//
+// Precision design:
+//  * Sources are stored in a spatially blocked sweep order (8^3 node
+//    blocks), so a tile of kTile32 consecutive sources is compact.  Each
+//    tile has an FP64 origin o; sources hold FP32 offsets x_s - o and every
+//    target forms x_t - o in FP64 before rounding, so the difference
+//    x_t - x_s of close pairs is exact to FP32 relative precision.
+//  * The phase k*rho is reduced in revolutions with k/(2 pi) split into a
+//    12-bit head kh and a tail kl: f = fma(rho, kh, -rint(rho*kh)) +
+//    rho*kl is exact to ~2^-24 before sin/cos run on the SFU.
+//  * The near-field test rho <= tau is decided in FP64 (with the FP64
+//    sweep's own arithmetic) whenever the FP32 rho^2 lies within 1e-4 of
+//    tau^2, so FP32 and FP64 operators classify every pair alike.
+//  * Per tile the contributions are summed in FP32, across tiles in FP64.
+// Each thread owns kTgt32 targets; TMA bulk copies stage source tiles in
+// shared memory, double-buffered on mbarriers with bounded waits.
+#include "hz_internal.cuh"
+#include "bulk_copy.cuh"
+
+namespace hz {
+namespace {
+
+struct Args32 {
+    int64_t n, npad;
+    float wave, kh, kl, scale;  // scale = sg / (4 pi)
+    float tau2, guard_lo, guard_hi;
+    double tau;
+    const float4 *pos, *nrm, *dens;
+    const double4_32a *origin, *tpos;
+    const int *perm;
+    const double4_32a *pos64;  // tube order (for the near-field guard)
+    const double *p_re, *p_im, *pt_re, *pt_im;
+    double *q_re, *q_im, *qt_re, *qt_im;
+    unsigned *err;
+};
+
+// dens[s] = (w p, pt) at sweep slot s, FP32.
+__global__ void prep32_kernel(int64_t npad, const int *__restrict__ perm, const float4 *__restrict__ nrm,
+                              const double4_32a *__restrict__ tpos, const double *__restrict__ p_re,
+                              const double *__restrict__ p_im, const double *__restrict__ pt_re,
+                              const double *__restrict__ pt_im, float4 *__restrict__ dens)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < npad; s += (int64_t)gridDim.x * blockDim.x) {
+        const int c = perm[s];
+        float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c >= 0) {
+            const double w = tpos[s].w;
+            if (p_re) {
+                v.x = (float)(w * p_re[c]);
+                v.y = (float)(w * p_im[c]);
+            }
+            if (pt_re) {
+                v.z = (float)pt_re[c];
+                v.w = (float)pt_im[c];
+            }
+        }
+        dens[s] = v;
+    }
+}
+
+template <int MODE, bool DIR>
+__global__ void __launch_bounds__(kThreads32, 2) sweep32_kernel(Args32 a)
+{
+    constexpr int TS = kTile32, NT = kThreads32, TG = kTgt32;
+    __shared__ alignas(128) float4 sp[2][TS];
+    __shared__ alignas(128) float4 sn[2][TS];
+    __shared__ alignas(128) float4 sd[2][TS];
+    __shared__ alignas(8) uint64_t bar[2];
+
+    const int64_t slot0 = (int64_t)blockIdx.x * NT * TG + threadIdx.x;
+    double4_32a tp[TG];
+    float3 tn[TG];
+    float treg[TG];
+    double accAr[TG], accAi[TG], accHr[TG], accHi[TG];
+#pragma unroll
+    for (int g = 0; g < TG; g++) {
+        const int64_t s = slot0 + (int64_t)g * NT;
+        tp[g] = a.tpos[s];
+        const float4 nn = a.nrm[s];
+        tn[g] = make_float3(nn.x, nn.y, nn.z);
+        treg[g] = a.pos[s].w;
+        accAr[g] = accAi[g] = accHr[g] = accHi[g] = 0.0;
+    }
+    const int64_t ntiles = a.npad / TS;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue = [&](int64_t tile, int buf) {
+        const int64_t base = tile * TS;
+        const uint32_t bytes = TS * sizeof(float4);
+        mbar_arrive_expect_tx(&bar[buf], 3 * bytes);
+        bulk_g2s(&sp[buf][0], a.pos + base, bytes, &bar[buf]);
+        bulk_g2s(&sn[buf][0], a.nrm + base, bytes, &bar[buf]);
+        bulk_g2s(&sd[buf][0], a.dens + base, bytes, &bar[buf]);
+    };
+    if (threadIdx.x == 0) issue(0, 0);
+    for (int64_t tile = 0; tile < ntiles; tile++) {
+        const int buf = (int)(tile & 1);
+        if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
+        const double4_32a o = a.origin[tile];
+        float3 rel[TG];
+#pragma unroll
+        for (int g = 0; g < TG; g++)
+            rel[g] = make_float3((float)(tp[g].x - o.x), (float)(tp[g].y - o.y), (float)(tp[g].z - o.z));
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, DEV_ERR_WAIT);
+                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
+            }
+            return;
+        }
+        float fAr[TG], fAi[TG], fHr[TG], fHi[TG];
+#pragma unroll
+        for (int g = 0; g < TG; g++) fAr[g] = fAi[g] = fHr[g] = fHi[g] = 0.f;
+#pragma unroll 2
+        for (int j = 0; j < TS; j++) {
+            const float4 s_p = sp[buf][j];
+            const float4 s_n = sn[buf][j];
+            const float4 s_d = sd[buf][j];
+#pragma unroll
+            for (int g = 0; g < TG; g++) {
+                const float dx = rel[g].x - s_p.x, dy = rel[g].y - s_p.y, dz = rel[g].z - s_p.z;
+                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+                bool near = r2 <= a.tau2;
+                if (r2 > a.guard_lo && r2 < a.guard_hi) {
+                    // decide exactly as the FP64 sweep does
+                    const int c = a.perm[tile * TS + j];
+                    if (c >= 0) {
+                        const double4_32a q = a.pos64[c];
+                        const double x1 = tp[g].x - q.x, x2 = tp[g].y - q.y, x3 = tp[g].z - q.z;
+                        near = !(sqrt(x1 * x1 + x2 * x2 + x3 * x3) > a.tau);
+                    }
+                }
+                const float rinv = rsqrtf(r2);
+                const float rho = r2 * rinv;
+                const float tt = rho * a.kh;
+                const float nn = rintf(tt);
+                float f = fmaf(rho, a.kh, -nn);
+                f = fmaf(rho, a.kl, f);
+                float S, C;
+                __sincosf(f * 6.28318530717958647692f, &S, &C);
+                const float u1 = fmaf(C, rinv, a.wave * S);   // k sin + cos/rho
+                const float u2 = fmaf(a.wave, C, -S * rinv);  // k cos - sin/rho
+                const float rr = rinv * rinv * a.scale;
+                const float a1 = -u1 * rr, a2 = u2 * rr;
+                const float pn = dx * s_n.x + dy * s_n.y + dz * s_n.z;        // (x_t-x_s).n_s
+                const float pt = dx * tn[g].x + dy * tn[g].y + dz * tn[g].z;  // (x_t-x_s).n_t
+                const float pA = DIR ? pn : pt, pH = DIR ? pt : pn;
+                float vAr = a1 * pA, vAi = a2 * pA, vHr = -a1 * pH, vHi = a2 * pH;
+                if (near) {
+                    vAr = DIR ? s_p.w : treg[g];
+                    vHr = DIR ? treg[g] : s_p.w;
+                    vAi = 0.f;
+                    vHi = 0.f;
+                }
+                if (MODE & SWEEP_A) {
+                    fAr[g] = fmaf(vAr, s_d.x, fmaf(-vAi, s_d.y, fAr[g]));
+                    fAi[g] = fmaf(vAr, s_d.y, fmaf(vAi, s_d.x, fAi[g]));
+                }
+                if (MODE & SWEEP_AH) {
+                    fHr[g] = fmaf(vHr, s_d.z, fmaf(-vHi, s_d.w, fHr[g]));
+                    fHi[g] = fmaf(vHr, s_d.w, fmaf(vHi, s_d.z, fHi[g]));
+                }
+            }
+        }
+#pragma unroll
+        for (int g = 0; g < TG; g++) {
+            accAr[g] += fAr[g];
+            accAi[g] += fAi[g];
+            accHr[g] += fHr[g];
+            accHi[g] += fHi[g];
+        }
+        __syncthreads();
+    }
+#pragma unroll
+    for (int g = 0; g < TG; g++) {
+        const int64_t s = slot0 + (int64_t)g * NT;
+        const int c = a.perm[s];
+        if (c < 0) continue;
+        if (MODE & SWEEP_A) {
+            if (!isfinite(accAr[g]) || !isfinite(accAi[g])) atomicOr(a.err, DEV_ERR_NONFINITE);
+            a.q_re[c] = accAr[g] + 0.5 * a.p_re[c];
+            a.q_im[c] = accAi[g] + 0.5 * a.p_im[c];
+        }
+        if (MODE & SWEEP_AH) {
+            const double w = tp[g].w;
+            const double r = w * accHr[g], i = w * accHi[g];
+            if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
+            a.qt_re[c] = r + 0.5 * a.pt_re[c];
+            a.qt_im[c] = i + 0.5 * a.pt_im[c];
+        }
+    }
+}
+
+template <int MODE>
+void launch32(const Args32 &a, bool dir, cudaStream_t s)
+{
+    const unsigned blocks = (unsigned)(a.npad / (kThreads32 * kTgt32));
+    if (dir) sweep32_kernel<MODE, true><<<blocks, kThreads32, 0, s>>>(a);
+    else sweep32_kernel<MODE, false><<<blocks, kThreads32, 0, s>>>(a);
+}
+
+}  // namespace
+
+// Split k/(2 pi) into a head with 12 significant bits and an FP32 tail.
+void split_wave(double wave, float &kh, float &kl)
+{
+    const double kc = wave / (2.0 * 3.14159265358979323846264338328);
+    int e;
+    frexp(kc, &e);
+    const double q = ldexp(1.0, e - 12);
+    const double head = nearbyint(kc / q) * q;
+    kh = (float)head;
+    kl = (float)(kc - head);
+}
+
+int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode, const double *p_re,
+              const double *p_im, const double *pt_re, const double *pt_im, double *q_re, double *q_im,
+              double *qt_re, double *qt_im, float4 *dens, cudaStream_t s)
+{
+    if (c.n <= 0) return HZ_OK;
+    const bool useA = (mode & SWEEP_A) != 0, useH = (mode & SWEEP_AH) != 0;
+    {
+        int dev = 0, sms = 152;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        long long b = (r.npad + 255) / 256;
+        if (b > sms * 8) b = sms * 8;
+        prep32_kernel<<<(unsigned)b, 256, 0, s>>>(r.npad, r.perm, r.nrm, r.tpos, useA ? p_re : nullptr,
+                                                  useA ? p_im : nullptr, useH ? pt_re : nullptr,
+                                                  useH ? pt_im : nullptr, dens);
+        HZ_CHECK_LAUNCH();
+    }
+    Args32 a;
+    a.n = c.n;
+    a.npad = r.npad;
+    a.wave = (float)c.wave;
+    split_wave(c.wave, a.kh, a.kl);
+    a.scale = (float)(((c.interior == 1) ? -1.0 : 1.0) / (4.0 * 3.14159265358979323846264338328));
+    a.tau = c.tau;
+    a.tau2 = (float)(c.tau * c.tau);
+    a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
+    a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
+    a.pos = r.pos;
+    a.nrm = r.nrm;
+    a.dens = dens;
+    a.origin = r.origin;
+    a.tpos = r.tpos;
+    a.perm = r.perm;
+    a.pos64 = pos64;
+    a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
+    a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
+    a.err = c.err;
+    if (mode == SWEEP_PAIR) launch32<SWEEP_PAIR>(a, c.dirichlet != 0, s);
+    else if (mode == SWEEP_A) launch32<SWEEP_A>(a, c.dirichlet != 0, s);
+    else launch32<SWEEP_AH>(a, c.dirichlet != 0, s);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
+}  // namespace hz

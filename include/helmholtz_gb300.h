@@ -1,0 +1,194 @@
+/*
+ * helmholtz_gb300.h -- C ABI of the GB300 (sm_103a) implicit-boundary-integral
+ * Helmholtz hot path.
+ *
+ * Everything here is plain C: pointers, sizes and status codes, no exits.
+ * Every call returns HZ_OK (0) or a negative HZ_ERR_* code; hz_last_error()
+ * gives the message of the last failure on the calling thread.
+ *
+ * Memory.  Arrays marked "where" are host pointers when where == HZ_HOST and
+ * device pointers (on the operator's device) when where == HZ_DEVICE.  The
+ * operator owns all device memory it allocates; host buffers stay owned by
+ * the caller, as in the reference, whose routines take caller-allocated
+ * arrays.  Calls on one operator are stream-ordered on its stream and must
+ * not be made concurrently from several threads.
+ *
+ * Layout.  Grids are contiguous (N+1)^3 FP64 arrays, node (i,j,k) at
+ * ((i*(N+1))+j)*(N+1)+k with coordinates (x,y,z) = (int_l + j*H,
+ * int_l + i*H, int_l + k*H): the flattening of the reference's ragged
+ * double*** grids (large3Dexample2.c:378-403,428-437).  Tube points are in
+ * the reference's lexicographic (i,j,k) order (large3Dexample2.c:548-597).
+ * Interleaved xyz arrays hold 3 doubles per point.  Complex vectors are
+ * passed as separate real and imaginary arrays, as the reference does
+ * (density / densityimg).
+ */
+#ifndef HELMHOLTZ_GB300_H
+#define HELMHOLTZ_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#define HZ_API __attribute__((visibility("default")))
+#else
+#define HZ_API
+#endif
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define HZ_OK 0
+#define HZ_ERR_ARG (-1)          /* invalid argument or size                    */
+#define HZ_ERR_CUDA (-2)         /* CUDA runtime error (no device, OOM, ...)    */
+#define HZ_ERR_STATE (-3)        /* call out of order (e.g. no tube built yet)  */
+#define HZ_ERR_GRID (-4)         /* projected point outside the grid; the
+                                    reference exits at interpolate3D.c:35       */
+#define HZ_ERR_NONFINITE (-5)    /* NaN/Inf in an input or result               */
+#define HZ_ERR_BREAKDOWN (-6)    /* Krylov breakdown (zero denominator)         */
+#define HZ_ERR_DEVICE_WAIT (-7)  /* a bounded device-side wait gave up          */
+
+#define HZ_HOST 0
+#define HZ_DEVICE 1
+
+/* Arithmetic of a matvec or solve. */
+#define HZ_PREC_F64 0         /* plain FP64 everywhere                                  */
+#define HZ_PREC_F32 1         /* FP32 pair sweep (tile-local origins, split phase),
+                                 FP64 inner products                                    */
+#define HZ_PREC_F32_REFINED 2 /* FP32 inner solves inside FP64 iterative refinement whose
+                                 residual b - A x uses the FP64 sweep                   */
+
+/* Krylov method. */
+#define HZ_BICG 0     /* complex BiCG with A and A^H: BICGSTAB.c:5-339 (CompBiCG)  */
+#define HZ_BICGSTAB 1 /* complex BiCGSTAB (the reference's real BiCGSTAB,
+                         large3Dexample2.c:2265-2477, in complex arithmetic)      */
+
+/* Evaluation layers. */
+#define HZ_SINGLE_LAYER 0 /* NeumannTest, large3Dexample2.c:1810-1824 */
+#define HZ_DOUBLE_LAYER 1 /* the Dirichlet matrix's kernel off the surface */
+
+/* Boundary data kinds for hz_rhs_point_source. */
+#define HZ_RHS_POINT_DIRICHLET 0 /* g = e^{ik|x-s|}/(4 pi |x-s|)                        */
+#define HZ_RHS_POINT_NEUMANN 1   /* dg/dn along the outward normal -n                   */
+#define HZ_RHS_MONOPOLE_NEUMANN 2 /* cal_partialu/img, large3Dexample2.c:4778,4840      */
+#define HZ_RHS_MONOPOLE_DIRICHLET 3 /* cal_u/cal_uimg, large3Dexample2.c:4642,4724     */
+
+/* Problem parameters: the reference's compile-time switches as runtime
+ * values (frame.h INT_L/INT_U, PDE.h FACTOR/TAU_FACTOR/DIRICHLET/
+ * INTERIOR_MODE, the driver's WAVE and N, weno_mode of main). */
+typedef struct hz_params {
+    int N;             /* cells per axis; the grid has (N+1)^3 nodes        */
+    double int_l;      /* domain lower bound (reference: -2.0)              */
+    double int_u;      /* domain upper bound (reference: 2.0)               */
+    double wave;       /* wave number k                                     */
+    double factor;     /* tube half-width eps = factor * H (reference: 2.0)  */
+    double tau_factor; /* regularisation radius tau = tau_factor * H (2.0)  */
+    int dirichlet;     /* 0: Neumann (single layer), 1: Dirichlet (double)  */
+    int interior;      /* 0: exterior problem, 1: interior                  */
+    int weno_order;    /* 5 (reference main) or 3                           */
+} hz_params;
+
+typedef struct hz_operator hz_operator;
+
+typedef struct hz_solve_opts {
+    int method;        /* HZ_BICG or HZ_BICGSTAB                                        */
+    int precision;     /* HZ_PREC_*                                                     */
+    double tol;        /* stop at ||b - A x|| / ||b|| < tol (reference DEFAULTACC 1e-7) */
+    int maxit;         /* Krylov iteration cap (reference: 2000)                        */
+    double inner_tol;  /* HZ_PREC_F32_REFINED: relative tolerance of each inner solve   */
+    int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap                      */
+    int stagnation;    /* 1: also stop when |delta(||r||/||b||)| < 1e-3 tol (reference) */
+} hz_solve_opts;
+
+typedef struct hz_solve_info {
+    int iterations;       /* Krylov iterations in total (inner ones when refined) */
+    int outer;            /* refinement steps (0 when not refined)                */
+    double resid;         /* final ||b - A x|| / ||b|| in the solve's own arithmetic */
+    double resid_f64;     /* final relative residual from an FP64 sweep (refined) */
+    double seconds;       /* wall time of the solve                               */
+    int64_t pair_evals;   /* kernel pair evaluations performed                    */
+    int status;           /* HZ_OK, or why it stopped early                       */
+} hz_solve_info;
+
+HZ_API const char *hz_last_error(void);
+
+/* Reference defaults: [-2,2]^3, FACTOR 2, TAU_FACTOR 2, Neumann, exterior,
+ * WENO5, N and wave as given. */
+HZ_API void hz_params_default(hz_params *p, int N, double wave);
+
+/* Operator lifetime.  hz_create selects the current CUDA device. */
+HZ_API int hz_create(const hz_params *p, hz_operator **out);
+HZ_API void hz_destroy(hz_operator *op);
+/* Run subsequent work on this cudaStream_t (NULL: the operator's own). */
+HZ_API int hz_set_stream(hz_operator *op, void *cuda_stream);
+HZ_API void *hz_get_stream(hz_operator *op);
+
+/* Upload the signed distance grid ((N+1)^3 doubles, d > 0 inside): the
+ * reference reads it from distance<N>.txt (large3Dexample2.c:405-424). */
+HZ_API int hz_set_distance(hz_operator *op, const double *d, int where);
+
+/* Level-set preprocessing on the device: WENO gradient
+ * (distance_application3D.c:56-140), curvatures (:35-53 over every node),
+ * tube (large3Dexample2.c:548-597) and per-point arrays (:4340-4452).
+ * Returns the tube size in *n. */
+HZ_API int hz_build(hz_operator *op, int64_t *n);
+HZ_API int64_t hz_tube_size(const hz_operator *op);
+
+/* Copy out grids (any pointer may be NULL). */
+HZ_API int hz_get_grids(hz_operator *op, double *gx, double *gy, double *gz, double *mcurv, double *gcurv,
+                 int where);
+/* Copy out tube arrays (any pointer may be NULL); xs/nrm are 3n interleaved. */
+HZ_API int hz_get_tube(hz_operator *op, int64_t *idx, double *xs, double *nrm, double *delta, double *jac,
+                double *reg, double *w, int where);
+
+/* q = A p (adjoint = 0) or q = A^H p (adjoint = 1): the matrix-free form of
+ * the dense products of large3Dexample2.c:3262-3309 with entries
+ * omp_get_Ccomp (:4463-4564). */
+HZ_API int hz_matvec(hz_operator *op, int precision, int adjoint, const double *p_re, const double *p_im,
+              double *q_re, double *q_im, int where);
+/* Fused q = A p and qt = A^H pt in one pass over the pairs (the two products
+ * of every BiCG iteration, :3262-3309). */
+HZ_API int hz_matvec_pair(hz_operator *op, int precision, const double *p_re, const double *p_im,
+                   const double *pt_re, const double *pt_im, double *q_re, double *q_im,
+                   double *qt_re, double *qt_im, int where);
+/* Multi right-hand side: Q = A P for nrhs column vectors stored one after
+ * the other (vector r at offset r*n), one kernel evaluation per pair. */
+HZ_API int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re,
+                    const double *p_im, double *q_re, double *q_im, int where);
+
+/* Solve A x = b (x0 = 0).  opts may be NULL: BiCG, FP64, tol 1e-7, 2000 its. */
+HZ_API int hz_solve(hz_operator *op, const hz_solve_opts *opts, const double *b_re, const double *b_im,
+             double *x_re, double *x_im, int where, hz_solve_info *info);
+HZ_API void hz_solve_opts_default(hz_solve_opts *o);
+
+/* Boundary data at the projected points (see HZ_RHS_*). src: 3 doubles. */
+HZ_API int hz_rhs_point_source(hz_operator *op, const double *src, int kind, double *b_re, double *b_im,
+                        int where);
+
+/* Field at m receivers (xyz interleaved, host or device per where) from the
+ * density sigma: single layer as NeumannTest (large3Dexample2.c:1810-1824)
+ * or the double layer of the Dirichlet formulation. */
+HZ_API int hz_eval(hz_operator *op, int layer, int64_t m, const double *rx, const double *s_re,
+            const double *s_im, double *u_re, double *u_im, int where);
+
+/* Whole-grid stencils without an operator.  d, outputs: (N+1)^3 doubles.
+ * hz_assign_gradient replaces ASSIGN_GRADIENT (distance_application3D.c:56);
+ * hz_assign_curvatures replaces the BothCurvs loop (large3Dexample2.c:446). */
+HZ_API int hz_assign_gradient(int N, double H, const double *d, double *gx, double *gy, double *gz,
+                       int weno_order, int where);
+HZ_API int hz_assign_curvatures(int N, double H, const double *d, double *mcurv, double *gcurv, int where);
+
+/* Dense complex BiCG on a caller-provided row-major n x n matrix (real and
+ * imaginary parts): the device form of CompBiCG (BICGSTAB.c:5-339). */
+HZ_API int hz_dense_bicg(int64_t n, const double *a_re, const double *a_im, const double *b_re,
+                  const double *b_im, double *x_re, double *x_im, double tol, int maxit,
+                  int where, hz_solve_info *info);
+
+/* Number of pair-sweep kernel launches and of all kernel launches made by
+ * this library in this process (for launch accounting). */
+HZ_API int64_t hz_kernel_launches(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,110 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures in tests/golden/ from the reference itself.
+
+Each case runs in its own process against oracle/_ref/libref_<variant>.so
+(the reference's C code, patched and compiled by oracle/build_ref.py), since
+the reference keeps its tube arrays in function statics.  Fixtures hold the
+input distance grid and the reference's outputs for it: WENO gradient and
+curvature grids, tube index list, per-point arrays, a sample of matrix
+entries, the dense products A p and A^H p for a seeded p, and the CompBiCG
+density for a point-source right-hand side solved to 1e-13.
+
+Usage:  python oracle/build_ref.py && python tests/golden/make_golden.py
+"""
+import json
+import os
+import subprocess
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+
+CASES = {
+    # reference defaults: [-2,2]^3, FACTOR 2, Neumann, exterior; sphere R=1
+    # offset from the grid nodes so no projection lands on a cell face.
+    "ref_neumann_sphere_n16": dict(variant="neumann", N=16, wave=2.0, shape="sphere", radius=1.0,
+                                   center=(0.013, 0.021, 0.007), rhs_kind=2),
+    "ref_neumann_sphere_n24": dict(variant="neumann", N=24, wave=5.0, shape="sphere", radius=1.0,
+                                   center=(0.013, 0.021, 0.007), rhs_kind=2),
+    # the BASELINE domain and formulation: [-1,1]^3, FACTOR 3, Dirichlet
+    "ref_dirichlet_sphere_n20": dict(variant="dirichlet", N=20, wave=5.0, shape="sphere", radius=0.5,
+                                     center=(0.0, 0.0, 0.0), rhs_kind=0),
+    # a torus small enough for a dense reference run (R=0.5, r=0.25 keeps
+    # the 3h tube inside the domain and away from the core circle at N=32)
+    "ref_dirichlet_torus_n32": dict(variant="dirichlet", N=32, wave=4.0, shape="torus", R=0.5, r=0.25,
+                                    rhs_kind=0),
+}
+
+
+def distance(case, int_l, int_u):
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    if case["shape"] == "sphere":
+        return G.sphere(case["N"], radius=case["radius"], center=case["center"], int_l=int_l, int_u=int_u)
+    return G.torus(case["N"], R=case["R"], r=case["r"], int_l=int_l, int_u=int_u)
+
+
+def run_case(name):
+    import oracle as O
+    case = CASES[name]
+    ref = O.Reference(case["variant"])
+    N, k = case["N"], case["wave"]
+    d = distance(case, ref.int_l, ref.int_u)
+    # silence the reference's printf chatter
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    ref.setup(N, k, d)
+    gx, gy, gz, mc, gc = ref.grids()
+    idx = ref.tube()
+    n = len(idx)
+    tp = ref.tube_points(n)
+    rng = np.random.default_rng(1234)
+    pi = rng.integers(0, n, 512).astype(np.int32)
+    pj = rng.integers(0, n, 512).astype(np.int32)
+    pi[:16] = pj[:16]
+    ent = ref.entries(n, pi, pj)
+    are, aim = ref.dense(n)
+    A = are + 1j * aim
+    p = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+    Ap = A @ p
+    AHp = A.conj().T @ p
+    orc = O.Oracle()
+    par = ref.params(N, k)
+    tpo = dict(xs=tp["xs"], nrm=tp["nrm"], w=tp["w"], reg=tp["reg"])
+    b = orc.rhs(par, tpo, np.zeros(3), case["rhs_kind"])
+    x = ref.compbicg(are, aim, b)
+    fi = rng.standard_normal((64, 7))
+    wv = np.array([ref.weno(f, 0.1, 5) for f in fi] + [ref.weno(f[:5], 0.1, 3) for f in fi])
+    meta = dict(name=name, N=N, wave=k, int_l=ref.int_l, int_u=ref.int_u, factor=ref.factor,
+                tau_factor=ref.tau_factor, dirichlet=ref.dirichlet, interior=ref.interior,
+                rhs_kind=case["rhs_kind"], n=n)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), d=d, gx=gx, gy=gy, gz=gz, mc=mc, gc=gc, idx=idx,
+                        xs=tp["xs"], nrm=tp["nrm"], delta=tp["delta"], jac=tp["jac"], reg=tp["reg"], w=tp["w"],
+                        pi=pi, pj=pj, entries=ent, p=p, Ap=Ap, AHp=AHp, b=b, x=x, weno_in=fi, weno_out=wv,
+                        meta=json.dumps(meta))
+    return name, n
+
+
+def main():
+    # One process per case: the reference exits (status 0) on some inputs and
+    # keeps per-process statics, so each case gets a fresh, time-limited child.
+    names = sys.argv[1:] or list(CASES)
+    for name in names:
+        out = os.path.join(HERE, name + ".npz")
+        if os.path.exists(out):
+            os.remove(out)
+        cmd = [sys.executable, os.path.abspath(__file__), "--one", name]
+        r = subprocess.run(cmd, timeout=1800)
+        if r.returncode != 0 or not os.path.exists(out):
+            raise SystemExit("case %s failed (exit %d, output %s)" % (name, r.returncode,
+                                                                   "present" if os.path.exists(out) else "missing"))
+        print(name, "ok")
+
+
+if __name__ == "__main__":
+    if len(sys.argv) == 3 and sys.argv[1] == "--one":
+        run_case(sys.argv[2])
+    else:
+        main()

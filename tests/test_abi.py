@@ -1,0 +1,68 @@
+"""The C-ABI library loads and exports every entry point declared in include/*.h
+(no compute: runs without a GPU)."""
+import os
+import re
+import subprocess
+
+import pytest
+
+from conftest import ROOT
+
+
+def declared(header, extern_c_only=True):
+    text = open(os.path.join(ROOT, "include", header)).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    names = re.findall(r"\b([A-Za-z_]\w*)\s*\(", text)
+    skip = {"if", "for", "while", "return", "sizeof", "defined"}
+    return sorted({n for n in names if n not in skip and not n.isupper() or n.startswith("hz_")})
+
+
+def exported(lib):
+    out = subprocess.run(["nm", "-D", "--defined-only", lib], capture_output=True, text=True, check=True).stdout
+    return {line.split()[-1] for line in out.splitlines() if line.strip()}
+
+
+def test_c_abi_symbols_exported(hz):
+    names = [n for n in declared("helmholtz_gb300.h") if n.startswith("hz_")]
+    assert len(names) >= 20
+    syms = exported(hz.LIB_PATH)
+    missing = [n for n in names if n not in syms]
+    assert not missing, missing
+    # and ctypes sees the same set with signatures
+    for n in names:
+        assert n in hz.SIGNATURES, n
+
+
+def test_reference_compat_symbols_exported(hz):
+    hdr = os.path.join(ROOT, "include", "helmholtz_ref_api.h")
+    if not os.path.exists(hdr):
+        pytest.skip("no reference-compatibility header")
+    syms = exported(hz.LIB_PATH)
+    demangled = subprocess.run(["nm", "-DC", "--defined-only", hz.LIB_PATH], capture_output=True, text=True,
+                               check=True).stdout
+    text = open(hdr).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    text = re.sub(r"//[^\n]*", "", text)
+    funcs = re.findall(r"^\s*(?:int|void|double)\s+([A-Za-z_]\w*)\s*\(", text, flags=re.M)
+    assert funcs
+    for f in funcs:
+        assert re.search(r"\b%s\(" % re.escape(f), demangled) or f in syms, f
+
+
+def test_errors_without_device(hz):
+    """Without a GPU the library reports an error instead of falling back."""
+    torch = pytest.importorskip("torch")
+    if torch.cuda.is_available():
+        pytest.skip("a GPU is present")
+    p = hz.params(16, 2.0)
+    with pytest.raises(hz.HzError) as e:
+        hz.Operator(p)
+    assert e.value.code == -2
+
+
+def test_bad_params_rejected(hz):
+    p = hz.params(4, 2.0)  # N below the supported minimum
+    with pytest.raises(hz.HzError) as e:
+        hz.Operator(p)
+    assert e.value.code == -1
