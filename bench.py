@@ -1,0 +1,317 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 IBIM Helmholtz hot path.
+
+Workload (the at-scale configuration of the reference's hot path): torus
+R=0.6, r=0.25 sampled as its analytic signed distance on a 256^3 grid over
+[-1,1]^3, tube |phi| <= 3h (n = 581,420 points), k = 20, Dirichlet
+(double-layer) formulation with point-source data from (0.6, 0, 0).
+
+A step is one iteration of the solver's hot loop: the fused FP32 pair sweep
+producing A p and A^H pt over all n^2 point pairs (TMA-staged tiles,
+tile-local origins, split phase), followed by the FP64 BiCG vector updates
+and inner products.  It counts 2 n^2 pair evaluations.  ``value`` is pair
+evaluations per second with the right-hand side resident in HBM; ``e2e`` is
+the same step through the public C ABI with host buffers (H2D of b, D2H of
+x inside the timed region).  L2 is flushed (256 MB write) between steps.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+``--impl reference`` times the reference's own CPU pair evaluation
+(omp_get_Ccomp + its complex multiply-add) on the host cores for the same
+workload (oracle/cpu_rate.py); with several ranks only rank 0 runs it.
+"""
+import argparse
+import csv
+import ctypes as C
+import io
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "256³ solve time & Gpair/s: FP32+FP64-refine vs plain FP64 GPU at 1e-6 rel err"
+FLOPS_PER_PAIR = 40  # reference pair formula, large3Dexample2.c:4471-4550
+# DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
+# 17.18 MB measured by ncu on the 128^3 torus (n = 145,272; see
+# profiles/sweep32_pair_torus_n128_full.md), scaled by n to n = 581,420.
+# The sweep reads every record once from DRAM and the tiles from L2, so
+# traffic grows in proportion to n.
+SWEEP32_TRAFFIC = 17.18e6 * 581420 / 145272
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--N", type=int, default=256)
+    ap.add_argument("--wave", type=float, default=20.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU time of one cpu_baseline step")
+    return ap.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(
+        os.environ.get("LOCAL_RANK", "0"))
+
+
+def workload_desc(N, wave, n):
+    return {"workload": "torus R=0.6 r=0.25, phi = analytic signed distance on %d^3 over [-1,1]^3, tube "
+                        "|phi|<=3h, k=%g, Dirichlet point source at (0.6,0,0); step = one BiCG iteration "
+                        "(fused FP32 A p + A^H pt sweep over all pairs + FP64 vector updates)" % (N, wave),
+            "N": N, "n_tube": n, "wave": wave, "pairs_per_step": 2 * n * n,
+            "l2": "flushed between steps by a 256 MB device write", "formulation": "dirichlet, exterior"}
+
+
+def cpu_rate(N, wave, impl, steps, warmup, step_seconds, timeout=900):
+    cmd = [sys.executable, os.path.join(ROOT, "oracle", "cpu_rate.py"), "--impl", impl, "--N", str(N), "--wave",
+           str(wave), "--steps", str(steps), "--warmup", str(warmup), "--step-seconds", str(step_seconds)]
+    r = subprocess.run(cmd, capture_output=True, text=True, timeout=timeout)
+    if r.returncode != 0:
+        raise RuntimeError("cpu_rate failed: %s" % r.stderr[-2000:])
+    line = [l for l in r.stdout.splitlines() if l.startswith("{")][-1]
+    return json.loads(line)
+
+
+class Clocks:
+    """Sample SM clocks and throttle reasons with nvidia-smi during a region."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.f = tempfile.NamedTemporaryFile(mode="w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def start(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.Q,
+                                       "--format=csv,noheader,nounits", "-lms", "200"], stdout=self.f,
+                                      stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+
+    def stop(self):
+        if self.p is None:
+            return None
+        self.p.terminate()
+        try:
+            self.p.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.p.kill()
+        self.f.flush()
+        rows = list(csv.reader(io.StringIO(open(self.f.name).read())))
+        os.unlink(self.f.name)
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for r in rows:
+            if len(r) < 9:
+                continue
+            try:
+                sm.append(float(r[1]))
+                mx.append(float(r[2]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, r[5:9]):
+                if v.strip().lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def run_reference(a, rank, world):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, min(6.0, 150.0 / max(1, a.steps + a.warmup)))
+    r = cpu_rate(a.N, a.wave, "auto", a.steps, a.warmup, per_step)
+    rates = r["pairs_per_s"]
+    total_pairs = r["pairs_per_step"] * len(rates)
+    total_s = sum(r["seconds_per_step"])
+    value = total_pairs / total_s / 1e9
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "Gpair/s", "n_gpus": a.gpus,
+        "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * total_s / len(rates),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": dict(workload_desc(a.N, a.wave, r["n"]),
+                       step="reference pair evaluation + complex MAC over %d target rows x all n sources "
+                            "(bounded sample of one A p product)" % r["rows"]),
+        "cpu_baseline": {"value": value, "unit": "Gpair/s", "cores": r["threads"],
+                         "kind": "reference" if r["impl"] == "reference" else "port",
+                         "sample": "%d rows x %d sources per step, %d steps; setup %.1f s untimed"
+                                   % (r["rows"], r["n"], len(rates), r["setup_s"])},
+        "e2e": {"value": value, "unit": "Gpair/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line))
+    sys.stdout.flush()
+    return 0
+
+
+def run_gb300(a, rank, world, local):
+    import numpy as np
+    import torch
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if dist is not None:
+            dist.barrier()
+
+    L = hz.load()
+    N, wave = a.N, a.wave
+    d = G.torus(N, R=0.6, r=0.25, int_l=-1.0, int_u=1.0)
+    p = hz.params(N, wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1)
+    stream = torch.cuda.Stream()
+    op = hz.Operator(p)
+    op.set_stream(stream.cuda_stream)
+    op.set_distance(d)
+    n = op.build()
+    b = op.rhs_point_source(np.array([0.6, 0.0, 0.0]), hz.RHS_POINT_DIRICHLET)
+    fp32_peak, fp64_peak = hz.measure_fma_peaks()
+
+    dev = torch.device("cuda", local)
+    b_re = torch.from_numpy(np.ascontiguousarray(b.real)).to(dev)
+    b_im = torch.from_numpy(np.ascontiguousarray(b.imag)).to(dev)
+    x_re = torch.empty(n, dtype=torch.float64, device=dev)
+    x_im = torch.empty(n, dtype=torch.float64, device=dev)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+    opts = hz.solve_opts(method=hz.BICG, precision=hz.PREC_F32, tol=1e-300, maxit=1, stagnation=0)
+    info = hz.SolveInfo()
+
+    def step(where, br, bi, xr, xi):
+        rc = L.hz_solve(op.h, C.byref(opts), br, bi, xr, xi, where, C.byref(info))
+        if rc != 0:
+            raise hz.HzError(rc, L.hz_last_error().decode())
+
+    dptr = (b_re.data_ptr(), b_im.data_ptr(), x_re.data_ptr(), x_im.data_ptr())
+    op.sweep_timing(1)
+    for _ in range(a.warmup):
+        with torch.cuda.stream(stream):
+            flush.fill_(1.0)
+        step(hz.HZ_DEVICE, *dptr)
+    torch.cuda.synchronize()
+    # ---------------- timed region: device-resident inputs
+    op.sweep_timing(1)  # reset the per-kernel totals (stays on: graphs keep their events)
+    launches0 = hz.kernel_launches()
+    clocks = Clocks(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0 = torch.cuda.Event(enable_timing=True)
+    ev1 = torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(_))
+        step(hz.HZ_DEVICE, *dptr)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    wall = time.perf_counter() - t0
+    barrier()
+    clk = clocks.stop()
+    launches = hz.kernel_launches() - launches0
+    dev_s = ev0.elapsed_time(ev1) / 1e3
+    sweep_ms, sweep_launches = op.sweep_timing(-1)
+    elapsed = max(dev_s, 1e-9)
+    if dist is not None:
+        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    pairs_step = 2 * n * n
+    value = pairs_step * a.steps * world / elapsed / 1e9
+
+    # ---------------- e2e: host buffers through the C ABI (H2D b, D2H x per step)
+    hb_re = torch.from_numpy(np.ascontiguousarray(b.real)).pin_memory()
+    hb_im = torch.from_numpy(np.ascontiguousarray(b.imag)).pin_memory()
+    hx_re = torch.empty(n, dtype=torch.float64).pin_memory()
+    hx_im = torch.empty(n, dtype=torch.float64).pin_memory()
+    hptr = (hb_re.data_ptr(), hb_im.data_ptr(), hx_re.data_ptr(), hx_im.data_ptr())
+    step(hz.HZ_HOST, *hptr)
+    torch.cuda.synchronize()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(a.steps):
+        with torch.cuda.stream(stream):
+            flush.fill_(float(_))
+        step(hz.HZ_HOST, *hptr)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    if dist is not None:
+        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = pairs_step * a.steps * world / e2e_s / 1e9
+
+    if rank != 0:
+        op.close()
+        return 0
+    avg_sweep_s = (sweep_ms / sweep_launches) / 1e3 if sweep_launches else None
+    achieved = pairs_step * FLOPS_PER_PAIR / avg_sweep_s / 1e12 if avg_sweep_s else None
+    line = {
+        "metric": METRIC, "value": value, "unit": "Gpair/s", "n_gpus": world, "steps": a.steps,
+        "warmup": a.warmup, "ms_per_step": 1e3 * elapsed / a.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic",
+        "config": workload_desc(N, wave, n),
+        "e2e": {"value": e2e, "unit": "Gpair/s", "h2d_bytes_per_step": 2 * n * 8, "d2h_bytes_per_step": 2 * n * 8,
+                "ms_per_step": 1e3 * e2e_s / a.steps},
+        "gpu_launches": launches,
+        "roofline": {"bound": "fp32", "kernel": "sweep32_kernel (fused A p + A^H pt)",
+                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                     "frac": (achieved / fp32_peak) if achieved else None, "traffic": SWEEP32_TRAFFIC,
+                     "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": pairs_step,
+                     "avg_launch_ms": avg_sweep_s * 1e3 if avg_sweep_s else None,
+                     "launches_timed": sweep_launches,
+                     "peak_source": "FP32 FFMA chains measured live on this GPU (hz_measure_fma_peaks)",
+                     "fp64_peak_tflops": fp64_peak},
+        "clocks": clk,
+        "wall_s": wall,
+    }
+    op.close()
+    if not a.no_cpu_baseline and world == 1:
+        try:
+            r = cpu_rate(N, wave, "auto", 2, 1, a.cpu_seconds)
+            v = sum(r["pairs_per_s"]) / len(r["pairs_per_s"]) / 1e9
+            line["cpu_baseline"] = {"value": v, "unit": "Gpair/s", "cores": r["threads"],
+                                    "kind": "reference" if r["impl"] == "reference" else "port",
+                                    "sample": "%d target rows x %d sources per step (%.2e pairs), 2 steps after 1 "
+                                              "warm-up, same 256^3 torus operator; setup %.1f s untimed"
+                                              % (r["rows"], r["n"], r["pairs_per_step"], r["setup_s"])}
+        except Exception as e:  # report, do not hide the GPU number
+            line["cpu_baseline"] = {"value": None, "unit": "Gpair/s", "error": str(e)[:300]}
+    print(json.dumps(line))
+    sys.stdout.flush()
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    a = parse()
+    rank, world, local = dist_env()
+    if a.impl == "reference":
+        return run_reference(a, rank, world)
+    return run_gb300(a, rank, world, local)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -78,6 +78,7 @@ SIGNATURES = {
     "hz_set_distance": ([_vp, _vp, C.c_int], C.c_int),
     "hz_build": ([_vp, C.POINTER(C.c_int64)], C.c_int),
     "hz_tube_size": ([_vp], C.c_int64),
+    "hz_sweep_timing": ([_vp, C.c_int, _dp, C.POINTER(C.c_int64)], C.c_int),
     "hz_get_grids": ([_vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_get_tube": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_matvec": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
@@ -92,6 +93,7 @@ SIGNATURES = {
     "hz_dense_bicg": ([C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
                        C.POINTER(SolveInfo)], C.c_int),
     "hz_kernel_launches": ([], C.c_int64),
+    "hz_measure_fma_peaks": ([_dp, _dp], C.c_int),
 }
 
 
@@ -146,6 +148,13 @@ def kernel_launches():
     return int(load().hz_kernel_launches())
 
 
+def measure_fma_peaks():
+    """(FP32, FP64) FMA throughput of the current GPU in TFLOP/s."""
+    a, b = C.c_double(), C.c_double()
+    _check(load().hz_measure_fma_peaks(C.byref(a), C.byref(b)))
+    return a.value, b.value
+
+
 class Operator:
     """Device-resident tube operator (one per surface and wave number)."""
 
@@ -190,6 +199,13 @@ class Operator:
         _check(load().hz_build(self.h, C.byref(n)))
         self.n = n.value
         return self.n
+
+    def sweep_timing(self, enable=-1):
+        """Enable (1) / disable (0) per-sweep CUDA-event timing, or read (-1):
+        returns (total device ms, launches) accumulated so far."""
+        ms, k = C.c_double(), C.c_int64()
+        _check(load().hz_sweep_timing(self.h, enable, C.byref(ms), C.byref(k)))
+        return ms.value, k.value
 
     def grids(self):
         S = self.p.N + 1

@@ -27,6 +27,7 @@ UNITS = {
     "krylov.cu": [],
     "evaluate.cu": [],
     "capi.cu": [],
+    "peaks.cu": [],
     "ref_api.cu": [],
 }
 

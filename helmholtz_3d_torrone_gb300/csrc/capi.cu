@@ -109,13 +109,50 @@ struct MatrixFreeOp final : LinOp {
               double *q_re, double *q_im, double *qt_re, double *qt_im, cudaStream_t s) override
     {
         const SweepConst c = sweep_const(op);
+        const int slot = op->timer.slot();
+        cudaEvent_t e0 = slot >= 0 ? op->timer.start[slot] : nullptr;
+        cudaEvent_t e1 = slot >= 0 ? op->timer.stop[slot] : nullptr;
         if (precision == HZ_PREC_F64)
             return sweep_f64(c, rec64(op), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im,
-                             op->scratch.as<double2>(), s);
+                             op->scratch.as<double2>(), s, e0, e1);
         return sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re,
-                         qt_im, op->dens32.as<float4>(), s);
+                         qt_im, op->dens32.as<float4>(), s, e0, e1);
+    }
+    void capture_begin() override { op->timer.next = 0; }
+    void capture_end() override
+    {
+        op->timer.graph_slots = op->timer.next;
+        op->timer.next = 0;
+    }
+    void iteration_done(bool graph) override
+    {
+        if (graph) {
+            op->timer.harvest(op->timer.graph_slots);
+        } else {
+            op->timer.harvest(op->timer.next);
+            op->timer.next = 0;
+        }
     }
 };
+
+int SweepTimer::slot()
+{
+    if (!on || next >= kSlots) return -1;
+    return next++;
+}
+
+void SweepTimer::harvest(int count)
+{
+    for (int i = 0; i < count && i < kSlots; i++) {
+        float ms = 0.f;
+        if (cudaEventElapsedTime(&ms, start[i], stop[i]) == cudaSuccess) {
+            total_ms += ms;
+            launches++;
+        } else {
+            cudaGetLastError();
+        }
+    }
+}
 
 struct DenseOp final : LinOp {
     int64_t n;
@@ -294,6 +331,10 @@ void hz_destroy(hz_operator *op)
     delete op->solver;
     op->solver = nullptr;
     if (op->own_stream) cudaStreamDestroy(op->own_stream);
+    for (int i = 0; i < SweepTimer::kSlots; i++) {
+        if (op->timer.start[i]) cudaEventDestroy(op->timer.start[i]);
+        if (op->timer.stop[i]) cudaEventDestroy(op->timer.stop[i]);
+    }
     delete op;
 }
 
@@ -394,6 +435,35 @@ int hz_build(hz_operator *op, int64_t *n_out)
 
 int64_t hz_tube_size(const hz_operator *op) { return op ? op->n : -1; }
 
+int hz_sweep_timing(hz_operator *op, int enable, double *total_ms, int64_t *launches)
+{
+    if (!op) {
+        set_error("operator is NULL");
+        return HZ_ERR_ARG;
+    }
+    if (total_ms) *total_ms = op->timer.total_ms;
+    if (launches) *launches = op->timer.launches;
+    if (enable >= 0) {
+        HZ_CHECK_CUDA(cudaSetDevice(op->device));
+        if (enable && !op->timer.start[0]) {
+            for (int i = 0; i < SweepTimer::kSlots; i++) {
+                HZ_CHECK_CUDA(cudaEventCreate(&op->timer.start[i]));
+                HZ_CHECK_CUDA(cudaEventCreate(&op->timer.stop[i]));
+            }
+        }
+        if ((enable != 0) != op->timer.on) {
+            // captured iteration graphs hold (or lack) the event nodes
+            op->solver->outer.invalidate_graph();
+            op->solver->inner.invalidate_graph();
+        }
+        op->timer.on = enable != 0;
+        op->timer.total_ms = 0.0;
+        op->timer.launches = 0;
+        op->timer.next = 0;
+    }
+    return HZ_OK;
+}
+
 int hz_get_grids(hz_operator *op, double *gx, double *gy, double *gz, double *mcurv, double *gcurv, int where)
 {
     HZ_TRY(need_built(op));
@@ -482,7 +552,9 @@ static int matvec_common(hz_operator *op, int precision, int mode, const double 
             HZ_TRY(stage_out(qt_im, dqt_im, n, where, s));
         }
     }
-    return check_device_error(op, "matvec");
+    const int rc = check_device_error(op, "matvec");
+    A.iteration_done(false);
+    return rc;
 }
 
 int hz_matvec(hz_operator *op, int precision, int adjoint, const double *p_re, const double *p_im, double *q_re,
@@ -594,6 +666,7 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
             HZ_TRY(A64.apply(SWEEP_A, x0, x1, nullptr, nullptr, q0, q1, nullptr, nullptr, s));
             HZ_TRY(vec_sub(n, b0, b1, q0, q1, r0, r1, s));
             HZ_TRY(vec_norm(n, r0, r1, part, dout, nr, s));
+            A64.iteration_done(false);
             const double prev = res;
             res = nr / normb;
             if (ist == HZ_ERR_BREAKDOWN && !(res < prev)) {

@@ -100,6 +100,21 @@ struct SweepConst {
 // sweep modes
 enum { SWEEP_A = 1, SWEEP_AH = 2, SWEEP_PAIR = 3 };
 
+// CUDA events around pair-sweep kernel launches, read back after the host
+// synchronises (also inside captured graphs, whose event-record nodes
+// re-record the same events on every replay).
+struct SweepTimer {
+    static constexpr int kSlots = 8;
+    bool on = false;
+    cudaEvent_t start[kSlots] = {}, stop[kSlots] = {};
+    int next = 0;         // slots recorded since the last harvest
+    int graph_slots = 0;  // slots recorded by the captured iteration graph
+    double total_ms = 0.0;
+    long long launches = 0;
+    int slot();           // next slot, or -1 when timing is off / full
+    void harvest(int count);
+};
+
 // stencils.cu
 int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
                          double *mc, double *gc, int order, cudaStream_t s);
@@ -118,12 +133,13 @@ int build_rec32(int64_t n, int64_t npad, const int *perm, const double4_32a *pos
 // sweep_f64.cu
 int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re, const double *p_im,
               const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
-              double *qt_im, double2 *scratch, cudaStream_t s);
+              double *qt_im, double2 *scratch, cudaStream_t s, cudaEvent_t ev0 = nullptr,
+              cudaEvent_t ev1 = nullptr);
 // sweep_f32.cu
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode,
               const double *p_re, const double *p_im, const double *pt_re, const double *pt_im,
               double *q_re, double *q_im, double *qt_re, double *qt_im, float4 *dens,
-              cudaStream_t s);
+              cudaStream_t s, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 
 }  // namespace hz
 
@@ -151,6 +167,7 @@ struct hz_operator {
     hz::DevBuf io;  // staging for host <-> device vectors
     hz::DevBuf dens32;
     hz_solver_state *solver = nullptr;  // Krylov workspaces (capi.cu)
+    hz::SweepTimer timer;
 };
 
 namespace hz {

@@ -482,8 +482,10 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
             cudaStream_t cs = s;
             bool captured = false;
             if (cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+                A.capture_begin();
                 int rc = (method == HZ_BICG) ? bicg_iteration(A, cs) : stab_iteration(A, cs);
                 cudaError_t e = cudaStreamEndCapture(cs, &g);
+                A.capture_end();
                 if (rc == HZ_OK && e == cudaSuccess && g) {
                     if (cudaGraphInstantiate(&graph_exec, g, 0) == cudaSuccess) captured = true;
                 }
@@ -509,6 +511,7 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
             HZ_TRY(method == HZ_BICG ? bicg_iteration(A, s) : stab_iteration(A, s));
         }
         HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+        A.iteration_done(exec != nullptr);
         iters = it;
         const double preerr = host_err[1];
         err = host_err[0];

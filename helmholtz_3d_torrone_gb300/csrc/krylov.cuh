@@ -11,6 +11,11 @@ struct LinOp {
     virtual int apply(int mode, const double *p_re, const double *p_im, const double *pt_re,
                       const double *pt_im, double *q_re, double *q_im, double *qt_re, double *qt_im,
                       cudaStream_t s) = 0;
+    // hooks for per-kernel timing around graph capture and after each
+    // synchronised iteration (graph: the iteration ran as a graph replay)
+    virtual void capture_begin() {}
+    virtual void capture_end() {}
+    virtual void iteration_done(bool graph) { (void)graph; }
 };
 
 struct KrylovScalars {

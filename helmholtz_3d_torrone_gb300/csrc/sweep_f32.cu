@@ -223,7 +223,8 @@ void split_wave(double wave, float &kh, float &kl)
 
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode, const double *p_re,
               const double *p_im, const double *pt_re, const double *pt_im, double *q_re, double *q_im,
-              double *qt_re, double *qt_im, float4 *dens, cudaStream_t s)
+              double *qt_re, double *qt_im, float4 *dens, cudaStream_t s, cudaEvent_t ev0,
+              cudaEvent_t ev1)
 {
     if (c.n <= 0) return HZ_OK;
     const bool useA = (mode & SWEEP_A) != 0, useH = (mode & SWEEP_AH) != 0;
@@ -258,10 +259,12 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
     a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
     a.err = c.err;
+    if (ev0) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev0, s, cudaEventRecordExternal));
     if (mode == SWEEP_PAIR) launch32<SWEEP_PAIR>(a, c.dirichlet != 0, s);
     else if (mode == SWEEP_A) launch32<SWEEP_A>(a, c.dirichlet != 0, s);
     else launch32<SWEEP_AH>(a, c.dirichlet != 0, s);
     HZ_CHECK_LAUNCH();
+    if (ev1) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev1, s, cudaEventRecordExternal));
     return HZ_OK;
 }
 

@@ -172,7 +172,8 @@ void launch64(const Args64 &a, bool dir, cudaStream_t s)
 
 int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re, const double *p_im,
               const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
-              double *qt_im, double2 *scratch, cudaStream_t s)
+              double *qt_im, double2 *scratch, cudaStream_t s, cudaEvent_t ev0,
+              cudaEvent_t ev1)
 {
     if (c.n <= 0) return HZ_OK;
     double4_32a *dens = reinterpret_cast<double4_32a *>(scratch);
@@ -198,10 +199,12 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
     a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
     a.err = c.err;
+    if (ev0) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev0, s, cudaEventRecordExternal));
     if (mode == SWEEP_PAIR) launch64<SWEEP_PAIR>(a, c.dirichlet != 0, s);
     else if (mode == SWEEP_A) launch64<SWEEP_A>(a, c.dirichlet != 0, s);
     else launch64<SWEEP_AH>(a, c.dirichlet != 0, s);
     HZ_CHECK_LAUNCH();
+    if (ev1) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev1, s, cudaEventRecordExternal));
     return HZ_OK;
 }
 

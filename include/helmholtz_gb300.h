@@ -134,6 +134,12 @@ HZ_API int hz_set_distance(hz_operator *op, const double *d, int where);
 HZ_API int hz_build(hz_operator *op, int64_t *n);
 HZ_API int64_t hz_tube_size(const hz_operator *op);
 
+/* Per-kernel timing of the pair sweeps: CUDA events recorded on the launch
+ * stream around every sweep kernel (also inside the solver's iteration
+ * graphs).  enable = 1 / 0 switches it on / off and clears the totals,
+ * enable = -1 only reads them: total device milliseconds and launches. */
+HZ_API int hz_sweep_timing(hz_operator *op, int enable, double *total_ms, int64_t *launches);
+
 /* Copy out grids (any pointer may be NULL). */
 HZ_API int hz_get_grids(hz_operator *op, double *gx, double *gy, double *gz, double *mcurv, double *gcurv,
                  int where);
@@ -184,9 +190,13 @@ HZ_API int hz_dense_bicg(int64_t n, const double *a_re, const double *a_im, cons
                   const double *b_im, double *x_re, double *x_im, double tol, int maxit,
                   int where, hz_solve_info *info);
 
-/* Number of pair-sweep kernel launches and of all kernel launches made by
- * this library in this process (for launch accounting). */
+/* Number of kernel launches made by this library in this process (graph
+ * launches count their kernels), for launch accounting. */
 HZ_API int64_t hz_kernel_launches(void);
+
+/* Measure the FP32 and FP64 FMA throughput of the current device (TFLOP/s,
+ * one FMA = 2 FLOP), the roofline denominators of the pair sweeps. */
+HZ_API int hz_measure_fma_peaks(double *fp32_tflops, double *fp64_tflops);
 
 #ifdef __cplusplus
 }

@@ -213,6 +213,7 @@ class Reference:
         L.ref_entries.argtypes = [C.c_int, C.c_int64, _i32p, _i32p, _dp, _dp]
         L.ref_dense_rows.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int]
         L.ref_compbicg.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_rows_matvec.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
         cfg = np.zeros(6)
         L.ref_config(_d(cfg))
         self.int_l, self.int_u, self.factor, self.tau_factor = cfg[:4]
@@ -266,6 +267,13 @@ class Reference:
         are, aim = np.empty((r1 - r0, n)), np.empty((r1 - r0, n))
         self.L.ref_dense_rows(n, r0, r1, _d(are), _d(aim), nthreads)
         return are, aim
+
+    def rows_matvec(self, n, v, r0, r1, nthreads=os.cpu_count() or 1):
+        vr = np.ascontiguousarray(v.real)
+        vi = np.ascontiguousarray(v.imag)
+        qr, qi = np.empty(r1 - r0), np.empty(r1 - r0)
+        self.L.ref_rows_matvec(n, r0, r1, _d(vr), _d(vi), _d(qr), _d(qi), nthreads)
+        return qr + 1j * qi
 
     def compbicg(self, are, aim, b):
         n = are.shape[0]

@@ -205,6 +205,28 @@ void ref_dense_rows(int n, int r0, int r1, double *are, double *aim, int nthread
     }
 }
 
+/* q = A p for rows [r0, r1): every entry from omp_get_Ccomp followed by the
+ * complex multiply-add of the reference's product loops (large3Dexample2.c:
+ * 3243-3244), i.e. one pair evaluation per (row, column).  Rows are spread
+ * over nthreads threads after the serial first call has built the arrays. */
+void ref_rows_matvec(int n, int r0, int r1, const double *pre, const double *pim, double *qre, double *qim,
+                     int nthreads)
+{
+    double eps = FACTOR * H, t[2];
+    omp_get_Ccomp(n, r0, 0, eps, t);
+#pragma omp parallel for schedule(dynamic, 1) num_threads(nthreads)
+    for (int i = r0; i < r1; i++) {
+        double tt[2], sr = 0.0, si = 0.0;
+        for (int k = 0; k < n; k++) {
+            omp_get_Ccomp(n, i, k, eps, tt);
+            sr += (tt[0] * pre[k] - tt[1] * pim[k]);
+            si += (tt[0] * pim[k] + tt[1] * pre[k]);
+        }
+        qre[i - r0] = sr;
+        qim[i - r0] = si;
+    }
+}
+
 /* CompBiCG (BICGSTAB.c:5-339) on a row-major dense matrix. */
 int ref_compbicg(int n, const double *are, const double *aim, const double *b, const double *bimg,
                  double *x, double *ximg)

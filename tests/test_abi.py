@@ -44,10 +44,24 @@ def test_reference_compat_symbols_exported(hz):
     text = open(hdr).read()
     text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
     text = re.sub(r"//[^\n]*", "", text)
-    funcs = re.findall(r"^\s*(?:int|void|double)\s+([A-Za-z_]\w*)\s*\(", text, flags=re.M)
+    funcs = re.findall(r"^\s*(?:HZ_API\s+)?(?:int|void|double)\s+([A-Za-z_]\w*)\s*\(", text, flags=re.M)
     assert funcs
     for f in funcs:
         assert re.search(r"\b%s\(" % re.escape(f), demangled) or f in syms, f
+    # link compatibility: the mangled names equal those of the reference's own
+    # objects (built by oracle/build_ref.py from the reference sources)
+    objdir = os.path.join(ROOT, "oracle", "_ref", "obj_neumann")
+    if os.path.isdir(objdir):
+        ref_syms = set()
+        for o in os.listdir(objdir):
+            out = subprocess.run(["nm", "--defined-only", os.path.join(objdir, o)], capture_output=True, text=True,
+                                 check=True).stdout
+            ref_syms |= {line.split()[-1] for line in out.splitlines() if line.strip()}
+        for f in funcs:
+            ours = [s for s in syms if re.fullmatch(r"_Z%d%s\w+" % (len(f), re.escape(f)), s)]
+            assert ours, f
+            if any(re.fullmatch(r"_Z%d%s\w+" % (len(f), re.escape(f)), s) for s in ref_syms):
+                assert set(ours) <= ref_syms, (f, ours)
 
 
 def test_errors_without_device(hz):
