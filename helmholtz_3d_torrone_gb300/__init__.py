@@ -25,6 +25,7 @@ PREC_F64, PREC_F32, PREC_F32_REFINED = 0, 1, 2
 BICG, BICGSTAB = 0, 1
 SINGLE_LAYER, DOUBLE_LAYER = 0, 1
 RHS_POINT_DIRICHLET, RHS_POINT_NEUMANN, RHS_MONOPOLE_NEUMANN, RHS_MONOPOLE_DIRICHLET = 0, 1, 2, 3
+NOALLOC_MAX_POINTS = 32768  # HZ_NOALLOC_MAX_POINTS
 
 ERRORS = {-1: "HZ_ERR_ARG", -2: "HZ_ERR_CUDA", -3: "HZ_ERR_STATE", -4: "HZ_ERR_GRID",
           -5: "HZ_ERR_NONFINITE", -6: "HZ_ERR_BREAKDOWN", -7: "HZ_ERR_DEVICE_WAIT"}
@@ -94,6 +95,8 @@ SIGNATURES = {
                        C.POINTER(SolveInfo)], C.c_int),
     "hz_kernel_launches": ([], C.c_int64),
     "hz_measure_fma_peaks": ([_dp, _dp], C.c_int),
+    "hz_matvec_f64_noalloc": ([C.POINTER(Params), C.c_int64, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                               _vp], C.c_int),
 }
 
 

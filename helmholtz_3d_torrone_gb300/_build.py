@@ -28,6 +28,7 @@ UNITS = {
     "evaluate.cu": [],
     "capi.cu": [],
     "peaks.cu": [],
+    "noalloc.cu": [],
     "ref_api.cu": [],
 }
 

@@ -194,6 +194,29 @@ HZ_API int hz_dense_bicg(int64_t n, const double *a_re, const double *a_im, cons
  * launches count their kernels), for launch accounting. */
 HZ_API int64_t hz_kernel_launches(void);
 
+/* Allocation-free FP64 product, for callers that cannot allocate device
+ * memory when they need it (applications that hand out all device memory
+ * from their own pools, plugin hosts that forbid allocation after start-up,
+ * loops that cannot afford cudaMalloc's implicit synchronisation).  It has
+ * no counterpart in the reference.  Computes q = A p (adjoint = 0) or
+ * q = A^H p (adjoint = 1) for the tube described by p (N, int_l, int_u,
+ * wave, tau_factor, dirichlet, interior are used) and the caller's device
+ * arrays xs, nrm (3n interleaved), reg, w, p, q (n each), as hz_get_tube
+ * returns them.  It calls no cudaMalloc, cudaFree or allocating library
+ * routine: its scratch is one fixed __device__ array of about 3 MiB that
+ * every GPU loading this library holds until the process exits; n above
+ * HZ_NOALLOC_MAX_POINTS is rejected with HZ_ERR_ARG.  The first call on a
+ * device looks up that array's address with that device current, so make
+ * the first call before any stream capture.  All calls share the array:
+ * calls that overlap on the GPU (other streams, other threads) race.  Work
+ * is ordered on `stream` (NULL: the legacy default stream) and the call
+ * waits for it to finish before returning its status. */
+#define HZ_NOALLOC_MAX_POINTS 32768
+HZ_API int hz_matvec_f64_noalloc(const hz_params *p, int64_t n, int adjoint, const double *xs,
+                                 const double *nrm, const double *reg, const double *w,
+                                 const double *p_re, const double *p_im, double *q_re, double *q_im,
+                                 void *stream);
+
 /* Measure the FP32 and FP64 FMA throughput of the current device (TFLOP/s,
  * one FMA = 2 FLOP), the roofline denominators of the pair sweeps. */
 HZ_API int hz_measure_fma_peaks(double *fp32_tflops, double *fp64_tflops);
