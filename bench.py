@@ -56,6 +56,19 @@ def parse():
     ap.add_argument("--wave", type=float, default=20.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--cpu-seconds", type=float, default=6.0, help="CPU time of one cpu_baseline step")
+    ap.add_argument("--solve", action="store_true",
+                    help="instead of the step benchmark, time complete solves (FP32+FP64 refinement at each "
+                         "--tol, FP64 BiCG iterations) and print one JSON line with solve times")
+    ap.add_argument("--tol", type=float, nargs="*", default=[1e-6, 1e-8])
+    ap.add_argument("--fp64-iters", type=int, default=1,
+                    help="--solve: timed plain-FP64 BiCG iterations (the full FP64 solve time is this "
+                         "per-iteration time x the iteration count; --fp64-full runs it to tolerance)")
+    ap.add_argument("--fp64-full", action="store_true")
+    ap.add_argument("--fp64-solve-iters", type=int, default=0,
+                    help="--solve: FP64 BiCG iteration count of a complete solve, for the extrapolated FP64 time")
+    ap.add_argument("--method", choices=["bicg", "gmres"], nargs="*", default=["bicg", "gmres"],
+                    help="--solve: inner Krylov method(s) of the refined solves")
+    ap.add_argument("--restart", type=int, default=40, help="--solve: GMRES restart length")
     return ap.parse_args()
 
 
@@ -305,11 +318,71 @@ def run_gb300(a, rank, world, local):
     return 0
 
 
+def run_solve(a, local):
+    """Complete solves on the benchmark workload: FP32 pair sweeps inside FP64
+    iterative refinement (BiCG), against plain FP64 BiCG."""
+    import numpy as np
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+
+    N, wave = a.N, a.wave
+    d = G.torus(N, R=0.6, r=0.25, int_l=-1.0, int_u=1.0)
+    p = hz.params(N, wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1)
+    out = {"mode": "solve", "config": workload_desc(N, wave, 0), "runs": []}
+    with hz.Operator(p) as op:
+        t0 = time.perf_counter()
+        op.set_distance(d)
+        n = op.build()
+        out["build_s"] = time.perf_counter() - t0
+        out["config"] = workload_desc(N, wave, n)
+        b = op.rhs_point_source(np.array([0.6, 0.0, 0.0]), hz.RHS_POINT_DIRICHLET)
+        sols = {}
+        for meth in a.method:
+            mid = hz.GMRES if meth == "gmres" else hz.BICG
+            for tol in a.tol:
+                x, info = op.solve(b, method=mid, precision=hz.PREC_F32_REFINED, tol=tol, inner_tol=1e-5,
+                                   restart=a.restart)
+                info.update(precision="f32+f64-refine", method=meth, tol=tol,
+                            gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
+                out["runs"].append(info)
+                sols[(meth, tol)] = x
+        # plain FP64 BiCG: per-iteration time (and, with --fp64-full, the whole solve)
+        if a.fp64_full:
+            tol = min(a.tol)
+            x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=tol)
+            info.update(precision="f64", tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
+            out["runs"].append(info)
+            for (meth, t), x in sols.items():
+                out.setdefault("rel_err_vs_f64", {})["%s %g" % (meth, t)] = float(
+                    np.max(np.abs(x - x64)) / np.max(np.abs(x64)))
+        elif a.fp64_iters > 0:
+            x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=1e-300, maxit=a.fp64_iters,
+                                 stagnation=0)
+            per_it = info["seconds"] / max(1, info["iterations"])
+            out["f64_per_iteration_s"] = per_it
+            out["f64_gpair_per_s"] = info["pair_evals"] / info["seconds"] / 1e9
+            if a.fp64_solve_iters:
+                out["f64_solve_s_extrapolated"] = per_it * a.fp64_solve_iters
+                out["f64_extrapolation"] = ("measured FP64 BiCG seconds per iteration x %d iterations (the FP64 "
+                                            "BiCG iteration count passed in, measured on a complete FP64 solve)"
+                                            % a.fp64_solve_iters)
+        for r in out["runs"]:
+            if r["precision"] != "f64" and "f64_solve_s_extrapolated" in out:
+                r["speedup_vs_f64_extrapolated"] = out["f64_solve_s_extrapolated"] / r["seconds"]
+    print(json.dumps(out))
+    sys.stdout.flush()
+    return 0
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
+    if a.solve:
+        import torch
+        torch.cuda.set_device(local)
+        return run_solve(a, local)
     return run_gb300(a, rank, world, local)
 
 

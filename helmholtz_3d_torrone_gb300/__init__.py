@@ -22,7 +22,7 @@ LIB_PATH = os.path.join(HERE, "libhzgb300.so")
 HZ_OK = 0
 HZ_HOST, HZ_DEVICE = 0, 1
 PREC_F64, PREC_F32, PREC_F32_REFINED = 0, 1, 2
-BICG, BICGSTAB = 0, 1
+BICG, BICGSTAB, GMRES = 0, 1, 2
 SINGLE_LAYER, DOUBLE_LAYER = 0, 1
 RHS_POINT_DIRICHLET, RHS_POINT_NEUMANN, RHS_MONOPOLE_NEUMANN, RHS_MONOPOLE_DIRICHLET = 0, 1, 2, 3
 NOALLOC_MAX_POINTS = 32768  # HZ_NOALLOC_MAX_POINTS
@@ -53,7 +53,7 @@ class Params(C.Structure):
 
 class SolveOpts(C.Structure):
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
-                ("inner_tol", C.c_double), ("max_outer", C.c_int), ("stagnation", C.c_int)]
+                ("inner_tol", C.c_double), ("max_outer", C.c_int), ("stagnation", C.c_int), ("restart", C.c_int)]
 
 
 class SolveInfo(C.Structure):
@@ -80,6 +80,8 @@ SIGNATURES = {
     "hz_build": ([_vp, C.POINTER(C.c_int64)], C.c_int),
     "hz_tube_size": ([_vp], C.c_int64),
     "hz_sweep_timing": ([_vp, C.c_int, _dp, C.POINTER(C.c_int64)], C.c_int),
+    "hz_autotune": ([_vp, C.POINTER(C.c_int), _dp], C.c_int),
+    "hz_set_sweep_config": ([_vp, C.c_int], C.c_int),
     "hz_get_grids": ([_vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_get_tube": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_matvec": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
@@ -87,14 +89,31 @@ SIGNATURES = {
     "hz_matvec_multi": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_solve": ([_vp, C.POINTER(SolveOpts), _vp, _vp, _vp, _vp, C.c_int, C.POINTER(SolveInfo)], C.c_int),
     "hz_solve_opts_default": ([C.POINTER(SolveOpts)], None),
+    "hz_solve_multi": ([_vp, C.POINTER(SolveOpts), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(SolveInfo),
+                        _vp], C.c_int),
+    "hz_rhs_plane_waves": ([_vp, C.c_int, _vp, C.c_int, _vp, _vp, C.c_int], C.c_int),
     "hz_rhs_point_source": ([_vp, _vp, C.c_int, _vp, _vp, C.c_int], C.c_int),
+    "hz_misfit_gradient": ([_vp, C.POINTER(SolveOpts), _vp, _vp, C.c_int, C.c_int64, _vp, _vp, _vp, _dp, _vp, _vp,
+                            _dp, _vp, C.c_int, C.POINTER(SolveInfo)], C.c_int),
     "hz_eval": ([_vp, C.c_int, C.c_int64, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_assign_gradient": ([C.c_int, C.c_double, _vp, _vp, _vp, _vp, C.c_int, C.c_int], C.c_int),
     "hz_assign_curvatures": ([C.c_int, C.c_double, _vp, _vp, _vp, C.c_int], C.c_int),
+    "hz_reinitialize": ([C.c_int, C.c_double, _vp, C.c_int, C.c_double, C.c_int, C.c_int], C.c_int),
     "hz_dense_bicg": ([C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
                        C.POINTER(SolveInfo)], C.c_int),
     "hz_kernel_launches": ([], C.c_int64),
     "hz_measure_fma_peaks": ([_dp, _dp], C.c_int),
+    "hz_eval_slice": ([_vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp,
+                       _vp, _vp, C.c_int], C.c_int),
+    "hz_reference_file_names": ([C.c_int, C.c_double, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p, C.c_char_p,
+                                 C.c_char_p, C.c_size_t], C.c_int),
+    "hz_read_distance_file": ([C.c_char_p, C.c_int, _vp], C.c_int),
+    "hz_write_distance_file": ([C.c_char_p, C.c_int, _vp], C.c_int),
+    "hz_write_rhs_files": ([C.c_char_p, C.c_char_p, C.c_int64, _vp, _vp], C.c_int),
+    "hz_read_rhs_files": ([C.c_char_p, C.c_char_p, C.c_int64, _vp, _vp], C.c_int),
+    "hz_write_density_files": ([C.c_char_p, C.c_char_p, C.c_int64, _vp, _vp], C.c_int),
+    "hz_read_density_files": ([C.c_char_p, C.c_char_p, C.c_int64, _vp, _vp], C.c_int),
+    "hz_write_result_file": ([C.c_char_p, C.c_double, C.c_double, C.c_double, C.c_double], C.c_int),
     "hz_matvec_f64_noalloc": ([C.POINTER(Params), C.c_int64, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                _vp], C.c_int),
 }
@@ -143,8 +162,8 @@ def params(N, wave, int_l=-2.0, int_u=2.0, factor=2.0, tau_factor=2.0, dirichlet
 
 
 def solve_opts(method=BICG, precision=PREC_F64, tol=1e-7, maxit=2000, inner_tol=1e-5, max_outer=20,
-               stagnation=1):
-    return SolveOpts(method, precision, tol, maxit, inner_tol, max_outer, stagnation)
+               stagnation=1, restart=40):
+    return SolveOpts(method, precision, tol, maxit, inner_tol, max_outer, stagnation, restart)
 
 
 def kernel_launches():
@@ -203,6 +222,15 @@ class Operator:
         self.n = n.value
         return self.n
 
+    def autotune(self):
+        """Pick the fastest FP32 sweep variant for this tube: (variant, ms)."""
+        cfg, ms = C.c_int(), C.c_double()
+        _check(load().hz_autotune(self.h, C.byref(cfg), C.byref(ms)))
+        return cfg.value, ms.value
+
+    def set_sweep_config(self, cfg):
+        _check(load().hz_set_sweep_config(self.h, cfg))
+
     def sweep_timing(self, enable=-1):
         """Enable (1) / disable (0) per-sweep CUDA-event timing, or read (-1):
         returns (total device ms, launches) accumulated so far."""
@@ -254,6 +282,53 @@ class Operator:
         _check(rc)
         return xr + 1j * xi, info.as_dict()
 
+    def solve_multi(self, B, opts=None, **kw):
+        """Solve for every row of B ([nrhs][n] complex); returns X, info, resid."""
+        opts = opts if opts is not None else solve_opts(**kw)
+        B = np.atleast_2d(B)
+        nrhs = B.shape[0]
+        br, bi = _f64(B.real), _f64(B.imag)
+        xr, xi = np.empty_like(br), np.empty_like(bi)
+        info = SolveInfo()
+        res = np.empty(nrhs)
+        _check(load().hz_solve_multi(self.h, C.byref(opts), nrhs, _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), HZ_HOST,
+                                     C.byref(info), _ptr(res)))
+        return xr + 1j * xi, info.as_dict(), res
+
+    def rhs_plane_waves(self, dirs, kind=RHS_POINT_DIRICHLET):
+        d = _f64(dirs).reshape(-1, 3)
+        m = d.shape[0]
+        br, bi = np.empty((m, self.n)), np.empty((m, self.n))
+        _check(load().hz_rhs_plane_waves(self.h, m, _ptr(d), kind, _ptr(br), _ptr(bi), HZ_HOST))
+        return br + 1j * bi
+
+    def evaluate_slice(self, sigma, axis=2, c=0.0, n2=64, lo=None, h2=None, layer=DOUBLE_LAYER, mask=0.0):
+        """Field on the plane axis = c (headless n2 x n2 buffer, row-major)."""
+        lo = self.p.int_l if lo is None else lo
+        h2 = (self.p.int_u - self.p.int_l) / (n2 - 1) if h2 is None else h2
+        sr, si = _f64(sigma.real), _f64(sigma.imag)
+        ur, ui = np.empty(n2 * n2), np.empty(n2 * n2)
+        _check(load().hz_eval_slice(self.h, layer, axis, c, n2, lo, h2, mask, _ptr(sr), _ptr(si), _ptr(ur), _ptr(ui),
+                                    HZ_HOST))
+        return (ur + 1j * ui).reshape(n2, n2)
+
+    def misfit_gradient(self, b, receivers, target, layer=None, opts=None, **kw):
+        """J = sum |u(x_m) - t_m|^2 and its adjoint gradients.
+
+        Returns (J, g, dJ_dk, dJ_dw, info) where g = dJ/dRe(b) + i dJ/dIm(b)."""
+        opts = opts if opts is not None else solve_opts(**kw)
+        layer = (DOUBLE_LAYER if self.p.dirichlet else SINGLE_LAYER) if layer is None else layer
+        br, bi = _f64(b.real), _f64(b.imag)
+        rx = _f64(receivers).reshape(-1, 3)
+        tr, ti = _f64(np.real(target)), _f64(np.imag(target))
+        J, dk = C.c_double(), C.c_double()
+        gr, gi, gw = np.empty(self.n), np.empty(self.n), np.empty(self.n)
+        info = SolveInfo()
+        _check(load().hz_misfit_gradient(self.h, C.byref(opts), _ptr(br), _ptr(bi), layer, rx.shape[0], _ptr(rx),
+                                         _ptr(tr), _ptr(ti), C.byref(J), _ptr(gr), _ptr(gi), C.byref(dk), _ptr(gw),
+                                         HZ_HOST, C.byref(info)))
+        return J.value, gr + 1j * gi, dk.value, gw, info.as_dict()
+
     def rhs_point_source(self, src, kind):
         s = _f64(src)
         br, bi = np.empty(self.n), np.empty(self.n)
@@ -285,6 +360,13 @@ def assign_curvatures(d, N, H):
     return m, g
 
 
+def reinitialize(phi, N, H, iters, cfl=0.5, weno_order=5):
+    """Device reinitialisation of a level set toward the signed distance."""
+    out = np.array(phi, dtype=np.float64, copy=True, order="C")
+    _check(load().hz_reinitialize(N, H, _ptr(out), iters, cfl, weno_order, HZ_HOST))
+    return out
+
+
 def dense_bicg(A, b, tol=1e-7, maxit=1000):
     """Device replacement of CompBiCG (BICGSTAB.c:5-339) on a dense matrix."""
     are, aim = _f64(A.real), _f64(A.imag)
@@ -295,3 +377,72 @@ def dense_bicg(A, b, tol=1e-7, maxit=1000):
     _check(load().hz_dense_bicg(n, _ptr(are), _ptr(aim), _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), tol, maxit,
                                 HZ_HOST, C.byref(info)))
     return xr + 1j * xi, info.as_dict()
+
+
+# ------------------------------------------------------------------ text files
+def reference_file_names(N, wave):
+    """Names the reference driver uses for distance, boundary data, density
+    and result files (large3Dexample2.c:407,607-608,2990-2991,1635)."""
+    bufs = [C.create_string_buffer(256) for _ in range(6)]
+    _check(load().hz_reference_file_names(N, wave, *bufs, 256))
+    keys = ["b", "bimg", "density", "densityimg", "result", "distance"]
+    return {k: b.value.decode() for k, b in zip(keys, bufs)}
+
+
+def read_distance_file(path, N):
+    d = np.empty((N + 1,) * 3)
+    _check(load().hz_read_distance_file(path.encode(), N, _ptr(d)))
+    return d
+
+
+def write_distance_file(path, N, d):
+    d = _f64(d)
+    _check(load().hz_write_distance_file(path.encode(), N, _ptr(d)))
+
+
+def write_rhs_files(path_re, path_im, b):
+    br, bi = _f64(b.real), _f64(b.imag)
+    _check(load().hz_write_rhs_files(path_re.encode(), path_im.encode(), len(br), _ptr(br), _ptr(bi)))
+
+
+def read_rhs_files(path_re, path_im, n):
+    br, bi = np.empty(n), np.empty(n)
+    _check(load().hz_read_rhs_files(path_re.encode(), path_im.encode(), n, _ptr(br), _ptr(bi)))
+    return br + 1j * bi
+
+
+def write_density_files(path_re, path_im, x):
+    xr, xi = _f64(x.real), _f64(x.imag)
+    _check(load().hz_write_density_files(path_re.encode(), path_im.encode(), len(xr), _ptr(xr), _ptr(xi)))
+
+
+def read_density_files(path_re, path_im, n):
+    xr, xi = np.empty(n), np.empty(n)
+    _check(load().hz_read_density_files(path_re.encode(), path_im.encode(), n, _ptr(xr), _ptr(xi)))
+    return xr + 1j * xi
+
+
+def write_result_file(path, exact, approx):
+    _check(load().hz_write_result_file(path.encode(), exact.real, exact.imag, approx.real, approx.imag))
+
+
+def misfit_function(op, receivers, target, layer=None, **solve_kw):
+    """A torch.autograd.Function over (Re b, Im b) for gradcheck of the
+    adjoint gradient against finite differences of the forward solve (used
+    by the tests only; the product entry point is Operator.misfit_gradient)."""
+    import torch
+
+    class _Misfit(torch.autograd.Function):
+        @staticmethod
+        def forward(ctx, b_re, b_im):
+            b = b_re.detach().cpu().numpy() + 1j * b_im.detach().cpu().numpy()
+            J, g, _, _, _ = op.misfit_gradient(b, receivers, target, layer=layer, **solve_kw)
+            ctx.save_for_backward(torch.from_numpy(g.real.copy()), torch.from_numpy(g.imag.copy()))
+            return torch.tensor(J, dtype=torch.float64)
+
+        @staticmethod
+        def backward(ctx, grad_out):
+            gr, gi = ctx.saved_tensors
+            return grad_out * gr, grad_out * gi
+
+    return _Misfit.apply

@@ -24,12 +24,17 @@ UNITS = {
     "tube.cu": ["-fmad=false"],
     "sweep_f64.cu": [],
     "sweep_f32.cu": [],
+    "sweep_multi.cu": [],
+    "krylov_multi.cu": [],
     "krylov.cu": [],
+    "gmres.cu": [],
     "evaluate.cu": [],
+    "adjoint.cu": [],
     "capi.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],
     "ref_api.cu": [],
+    "textio.cpp": [],
 }
 
 

@@ -1,6 +1,7 @@
 // capi.cu -- the extern "C" boundary (include/helmholtz_gb300.h).
 #include "hz_internal.cuh"
 #include "krylov.cuh"
+#include "krylov_multi.cuh"
 
 #include <atomic>
 #include <chrono>
@@ -9,6 +10,7 @@
 #include <cstdio>
 #include <cstring>
 #include <new>
+#include <vector>
 
 namespace hz {
 
@@ -55,6 +57,20 @@ int launch_eval(int64_t n, const double4_32a *pos, const double4_32a *nrm, const
                 double *u_im, cudaStream_t s);
 int launch_rhs(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *src, double wave, int kind,
                double *b_re, double *b_im, cudaStream_t s);
+int launch_eval_adjoint(int64_t n, const double4_32a *pos, const double4_32a *nrm, int64_t m, const double *rx,
+                        const double *r_re, const double *r_im, double wave, double tau, int interior, int layer,
+                        double *s_re, double *s_im, cudaStream_t s);
+int launch_eval_dk(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *s_re,
+                   const double *s_im, int64_t m, const double *rx, double wave, double tau, int interior, int layer,
+                   double *u_re, double *u_im, cudaStream_t s);
+int launch_sweep_dk(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *dreg,
+                    const double *s_re, const double *s_im, double wave, double tau, int interior, int dirichlet,
+                    double *q_re, double *q_im, cudaStream_t s);
+int launch_slice(int axis, double c, int n2, double lo, double h2, double mask, int N, double H, double int_l,
+                 const double *d, double *rx, unsigned char *keep, cudaStream_t s);
+int launch_mask(int64_t m, const unsigned char *keep, double *u_re, double *u_im, cudaStream_t s);
+int launch_plane_waves(int64_t n, const double4_32a *pos, const double4_32a *nrm, int ndir, const double *dirs,
+                       double wave, int kind, double *b_re, double *b_im, cudaStream_t s);
 size_t dense_partial_elems(int64_t n);
 int launch_dense(int64_t n, const double *are, const double *aim, const double *p_re, const double *p_im,
                  const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
@@ -116,7 +132,7 @@ struct MatrixFreeOp final : LinOp {
             return sweep_f64(c, rec64(op), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im,
                              op->scratch.as<double2>(), s, e0, e1);
         return sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re,
-                         qt_im, op->dens32.as<float4>(), s, e0, e1);
+                         qt_im, op->dens32.as<float4>(), s, e0, e1, op->sweep_cfg);
     }
     void capture_begin() override { op->timer.next = 0; }
     void capture_end() override
@@ -132,6 +148,10 @@ struct MatrixFreeOp final : LinOp {
             op->timer.harvest(op->timer.next);
             op->timer.next = 0;
         }
+    }
+    uint64_t key() const override
+    {
+        return ((uint64_t)(uintptr_t)op << 8) ^ (uint64_t)(precision * 16 + op->sweep_cfg) ^ 1ull;
     }
 };
 
@@ -165,17 +185,38 @@ struct DenseOp final : LinOp {
                             (mode & SWEEP_AH) ? pt_re : nullptr, pt_im, q_re, q_im, qt_re, qt_im, part_re, part_im,
                             s);
     }
+    uint64_t key() const override { return ((uint64_t)(uintptr_t)are << 4) ^ 2ull; }
+};
+
+// Multi right-hand-side operator over the tube.
+struct MultiMatrixFreeOp final : MultiOp {
+    hz_operator *op;
+    int precision;
+    DevBuf *scratch;
+    MultiMatrixFreeOp(hz_operator *o, int prec, DevBuf *sc) : op(o), precision(prec), scratch(sc) {}
+    int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im, cudaStream_t s) override
+    {
+        HZ_TRY(scratch->ensure(multi_rhs_scratch_bytes(op->n, op->r32.npad)));
+        return sweep_multi(sweep_const(op), op->r32, rec64(op), precision, R, p_re, p_im, q_re, q_im, scratch->ptr, s);
+    }
 };
 
 }  // namespace hz
 
 using namespace hz;
 
+// An inner FP32 solve stops after this many iterations without a new
+// minimum residual: rounding the densities to FP32 bounds what it can reach.
+constexpr int kInnerStall = 30;
+
 // Per-operator solver state (kept out of the public struct layout).
 struct hz_solver_state {
     Krylov outer, inner;
+    KrylovMulti multi;
     DevBuf vec;  // b, x, r, q (re/im) for refinement
     DevBuf small;
+    DevBuf mvec, mscratch;  // multi right-hand side staging and sweep scratch
+    DevBuf gwork, gsmall, gx;  // GMRES basis, Hessenberg partials, inner solution
 };
 
 namespace {
@@ -279,6 +320,7 @@ void hz_solve_opts_default(hz_solve_opts *o)
     o->inner_tol = 1e-5;
     o->max_outer = 20;
     o->stagnation = 1;
+    o->restart = 40;
 }
 
 int hz_create(const hz_params *p, hz_operator **out)
@@ -390,13 +432,14 @@ int hz_build(hz_operator *op, int64_t *n_out)
     const size_t nn = (size_t)(n > 0 ? n : 1);
     HZ_TRY(op->xs.ensure(3 * nn * sizeof(double)));
     HZ_TRY(op->nrm.ensure(3 * nn * sizeof(double)));
-    for (DevBuf *b : {&op->delta, &op->jac, &op->reg, &op->w}) HZ_TRY(b->ensure(nn * sizeof(double)));
+    for (DevBuf *b : {&op->delta, &op->jac, &op->reg, &op->w, &op->dreg}) HZ_TRY(b->ensure(nn * sizeof(double)));
     HZ_TRY(op->pos64.ensure(nn * sizeof(double4_32a)));
     HZ_TRY(op->nrm64.ensure(nn * sizeof(double4_32a)));
     HZ_TRY(tube_init(op->p, op->d.as<double>(), op->gx.as<double>(), op->gy.as<double>(), op->gz.as<double>(),
                      op->mc.as<double>(), op->gc.as<double>(), n, op->idx.as<int64_t>(), op->xs.as<double>(),
                      op->nrm.as<double>(), op->delta.as<double>(), op->jac.as<double>(), op->reg.as<double>(),
-                     op->w.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->err.as<unsigned>(), s));
+                     op->w.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->err.as<unsigned>(), s,
+                     op->dreg.as<double>()));
     HZ_TRY(check_device_error(op, "hz_build"));
     // FP32 sweep records in blocked order
     const int64_t unit = (int64_t)kThreads32 * kTgt32;  // multiple of kTile32
@@ -412,7 +455,7 @@ int hz_build(hz_operator *op, int64_t *n_out)
         HZ_TRY(sweep_order(N, n, op->idx.as<int64_t>(), op->perm.as<int>(), npad, op->scratch, s));
         HZ_TRY(build_rec32(n, npad, op->perm.as<int>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
                            op->pos32.as<float4>(), op->nrm32.as<float4>(), op->origin32.as<double4_32a>(),
-                           op->tpos32.as<double4_32a>(), s));
+                           op->tpos32.as<double4_32a>(), sweep32_reg_scale(op->p.interior), s));
     }
     op->r32.perm = op->perm.as<int>();
     op->r32.pos = op->pos32.as<float4>();
@@ -434,6 +477,70 @@ int hz_build(hz_operator *op, int64_t *n_out)
 }
 
 int64_t hz_tube_size(const hz_operator *op) { return op ? op->n : -1; }
+
+int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep)
+{
+    HZ_TRY(need_built(op));
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    const size_t n = (size_t)op->n;
+    if (n == 0) {
+        if (chosen) *chosen = op->sweep_cfg;
+        return HZ_OK;
+    }
+    // unit densities in the staging buffer (values do not change the timing)
+    double *io = op->io.as<double>();
+    HZ_CHECK_CUDA(cudaMemsetAsync(io, 0, 8 * n * sizeof(double), s));
+    cudaEvent_t e0, e1;
+    HZ_CHECK_CUDA(cudaEventCreate(&e0));
+    HZ_CHECK_CUDA(cudaEventCreate(&e1));
+    const SweepConst c = sweep_const(op);
+    int best = 0;
+    float best_ms = 1e30f;
+    int rc = HZ_OK;
+    for (int cfg = 0; cfg < sweep32_num_configs() && rc == HZ_OK; cfg++) {
+        float ms_min = 1e30f;
+        for (int rep = 0; rep < 2 && rc == HZ_OK; rep++) {
+            rc = sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), SWEEP_PAIR, io, io + n, io + 2 * n, io + 3 * n,
+                           io + 4 * n, io + 5 * n, io + 6 * n, io + 7 * n, op->dens32.as<float4>(), s, e0, e1, cfg);
+            if (rc == HZ_OK && cudaEventSynchronize(e1) == cudaSuccess) {
+                float ms = 0.f;
+                cudaEventElapsedTime(&ms, e0, e1);
+                if (ms < ms_min) ms_min = ms;
+            }
+        }
+        if (ms_min < best_ms) {
+            best_ms = ms_min;
+            best = cfg;
+        }
+    }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    if (rc != HZ_OK) return rc;
+    HZ_TRY(check_device_error(op, "hz_autotune"));
+    if (best != op->sweep_cfg) {
+        op->sweep_cfg = best;
+        op->solver->outer.invalidate_graph();
+        op->solver->inner.invalidate_graph();
+    }
+    if (chosen) *chosen = best;
+    if (ms_per_sweep) *ms_per_sweep = best_ms;
+    return HZ_OK;
+}
+
+int hz_set_sweep_config(hz_operator *op, int cfg)
+{
+    if (!op || cfg < 0 || cfg >= sweep32_num_configs()) {
+        set_error("hz_set_sweep_config: config must be in [0, %d)", sweep32_num_configs());
+        return HZ_ERR_ARG;
+    }
+    if (cfg != op->sweep_cfg) {
+        op->sweep_cfg = cfg;
+        op->solver->outer.invalidate_graph();
+        op->solver->inner.invalidate_graph();
+    }
+    return HZ_OK;
+}
 
 int hz_sweep_timing(hz_operator *op, int enable, double *total_ms, int64_t *launches)
 {
@@ -576,13 +683,293 @@ int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re
                     double *q_re, double *q_im, int where)
 {
     HZ_TRY(need_built(op));
-    if (nrhs < 1) {
-        set_error("nrhs must be >= 1");
+    HZ_TRY(where_ok(where));
+    if (nrhs < 1 || precision < HZ_PREC_F64 || precision > HZ_PREC_F32_REFINED) {
+        set_error("hz_matvec_multi: nrhs must be >= 1 and precision valid");
         return HZ_ERR_ARG;
     }
-    const size_t n = (size_t)op->n;
-    for (int r = 0; r < nrhs; r++)
-        HZ_TRY(hz_matvec(op, precision, 0, p_re + r * n, p_im + r * n, q_re + r * n, q_im + r * n, where));
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    hz_solver_state *st = op->solver;
+    const size_t n = (size_t)op->n, tot = n * (size_t)nrhs;
+    if (n == 0) return HZ_OK;
+    const double *dpr = p_re, *dpi = p_im;
+    double *dqr = q_re, *dqi = q_im;
+    if (where == HZ_HOST) {
+        HZ_TRY(st->mvec.ensure(4 * tot * sizeof(double)));
+        double *b = st->mvec.as<double>();
+        HZ_TRY(stage_in(b, p_re, tot, where, s));
+        HZ_TRY(stage_in(b + tot, p_im, tot, where, s));
+        dpr = b;
+        dpi = b + tot;
+        dqr = b + 2 * tot;
+        dqi = b + 3 * tot;
+    }
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    MultiMatrixFreeOp A(op, precision == HZ_PREC_F64 ? HZ_PREC_F64 : HZ_PREC_F32, &st->mscratch);
+    HZ_TRY(A.apply(nrhs, dpr, dpi, dqr, dqi, s));
+    if (where == HZ_HOST) {
+        HZ_TRY(stage_out(q_re, dqr, tot, where, s));
+        HZ_TRY(stage_out(q_im, dqi, tot, where, s));
+    }
+    return check_device_error(op, "hz_matvec_multi");
+}
+
+int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, const double *b_re, const double *b_im,
+                   double *x_re, double *x_im, int where, hz_solve_info *info, double *resid)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    hz_solve_opts o;
+    if (opts_in) o = *opts_in;
+    else hz_solve_opts_default(&o);
+    if (nrhs < 1 || !(o.tol > 0) || o.maxit < 1 || o.precision < HZ_PREC_F64 || o.precision > HZ_PREC_F32_REFINED) {
+        set_error("hz_solve_multi: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    hz_solver_state *st = op->solver;
+    const int64_t n = op->n;
+    const size_t tot = (size_t)n * (size_t)nrhs;
+    hz_solve_info inf{};
+    auto t0 = std::chrono::steady_clock::now();
+    std::vector<double> res(nrhs, 0.0);
+    if (n == 0) {
+        if (info) *info = inf;
+        return HZ_OK;
+    }
+    // staging: b, x, r, q  ([R][n] each, re/im)
+    HZ_TRY(st->mvec.ensure(8 * tot * sizeof(double)));
+    double *B0 = st->mvec.as<double>(), *B1 = B0 + tot, *X0 = B0 + 2 * tot, *X1 = B0 + 3 * tot, *R0 = B0 + 4 * tot,
+           *R1 = B0 + 5 * tot, *Q0 = B0 + 6 * tot, *Q1 = B0 + 7 * tot;
+    HZ_TRY(stage_in(B0, b_re, tot, where, s));
+    HZ_TRY(stage_in(B1, b_im, tot, where, s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    HZ_TRY(st->multi.reserve(n, nrhs));
+    int iters = 0, outer = 0;
+    long long pairs = 0;
+    const int blocks = (nrhs + multi_rhs_block() - 1) / multi_rhs_block();
+    if (o.precision != HZ_PREC_F32_REFINED) {
+        MultiMatrixFreeOp A(op, o.precision, &st->mscratch);
+        HZ_TRY(st->multi.solve(A, B0, B1, o.tol, o.maxit, o.stagnation != 0, s, iters, res));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(X0, st->multi.re(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(X1, st->multi.im(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        pairs = 2LL * iters * n * n * blocks;
+    } else {
+        // FP64 iterative refinement of every column: X += ||r_j|| A32^{-1} (r_j/||r_j||)
+        MultiMatrixFreeOp A32(op, HZ_PREC_F32, &st->mscratch), A64(op, HZ_PREC_F64, &st->mscratch);
+        HZ_TRY(st->small.ensure(vec_partial_bytes() + 64));
+        double *part = st->small.as<double>();
+        double *dout = part + (vec_partial_bytes() / sizeof(double));
+        std::vector<double> normb(nrhs), nr(nrhs);
+        for (int r = 0; r < nrhs; r++) HZ_TRY(vec_norm(n, B0 + r * n, B1 + r * n, part, dout, normb[r], s));
+        HZ_CHECK_CUDA(cudaMemsetAsync(X0, 0, tot * sizeof(double), s));
+        HZ_CHECK_CUDA(cudaMemsetAsync(X1, 0, tot * sizeof(double), s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(R0, B0, tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(R1, B1, tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        nr = normb;
+        for (int r = 0; r < nrhs; r++) res[r] = normb[r] > 0 ? 1.0 : 0.0;
+        auto worst = [&]() {
+            double w = 0;
+            for (double v : res) w = v > w ? v : w;
+            return w;
+        };
+        while (worst() >= o.tol && outer < o.max_outer) {
+            outer++;
+            for (int r = 0; r < nrhs; r++)
+                HZ_TRY(vec_scale(n, nr[r] > 0 ? 1.0 / nr[r] : 0.0, R0 + r * n, R1 + r * n, Q0 + r * n, Q1 + r * n, s));
+            int it = 0;
+            std::vector<double> ires;
+            HZ_TRY(st->multi.solve(A32, Q0, Q1, o.inner_tol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStall));
+            iters += it;
+            pairs += 2LL * it * n * n * blocks;
+            for (int r = 0; r < nrhs; r++)
+                HZ_TRY(vec_axpy(n, nr[r], st->multi.re(KrylovMulti::X) + r * n, st->multi.im(KrylovMulti::X) + r * n,
+                                X0 + r * n, X1 + r * n, s));
+            HZ_TRY(A64.apply(nrhs, X0, X1, Q0, Q1, s));
+            pairs += (long long)n * n * blocks;
+            HZ_TRY(vec_sub((int64_t)tot, B0, B1, Q0, Q1, R0, R1, s));
+            for (int r = 0; r < nrhs; r++) {
+                HZ_TRY(vec_norm(n, R0 + r * n, R1 + r * n, part, dout, nr[r], s));
+                res[r] = normb[r] > 0 ? nr[r] / normb[r] : 0.0;
+            }
+        }
+    }
+    HZ_TRY(stage_out(x_re, X0, tot, where, s));
+    HZ_TRY(stage_out(x_im, X1, tot, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    const int rc = check_device_error(op, "hz_solve_multi");
+    double worst = 0;
+    for (int r = 0; r < nrhs; r++) {
+        worst = res[r] > worst ? res[r] : worst;
+        if (resid) resid[r] = res[r];
+    }
+    inf.iterations = iters;
+    inf.outer = outer;
+    inf.resid = worst;
+    inf.resid_f64 = (o.precision == HZ_PREC_F32) ? -1.0 : worst;
+    inf.pair_evals = pairs;
+    inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+    inf.status = rc;
+    if (info) *info = inf;
+    return rc;
+}
+
+int hz_rhs_plane_waves(hz_operator *op, int ndir, const double *dirs, int kind, double *b_re, double *b_im,
+                       int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    if (ndir < 1 || !dirs || (kind != HZ_RHS_POINT_DIRICHLET && kind != HZ_RHS_POINT_NEUMANN)) {
+        set_error("hz_rhs_plane_waves: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    cudaStream_t s = op->stream;
+    const size_t n = (size_t)op->n, tot = n * (size_t)ndir;
+    hz_solver_state *st = op->solver;
+    DevBuf dd;
+    HZ_TRY(dd.ensure(3 * (size_t)ndir * sizeof(double)));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(dd.ptr, dirs, 3 * (size_t)ndir * sizeof(double), cudaMemcpyHostToDevice, s));
+    double *dre = b_re, *dim = b_im;
+    if (where == HZ_HOST) {
+        HZ_TRY(st->mvec.ensure(2 * tot * sizeof(double)));
+        dre = st->mvec.as<double>();
+        dim = dre + tot;
+    }
+    HZ_TRY(launch_plane_waves(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), ndir, dd.as<double>(),
+                              op->p.wave, kind, dre, dim, s));
+    if (where == HZ_HOST) {
+        HZ_TRY(stage_out(b_re, dre, tot, where, s));
+        HZ_TRY(stage_out(b_im, dim, tot, where, s));
+    }
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+// Solve A x = b (adjoint = false) or A^H x = b (adjoint = true) with the
+// options o; b and x are device vectors (x must not alias the solver's
+// workspace).  Fills inf; returns HZ_OK or an error, status in *status.
+static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, const double *b0, const double *b1,
+                        double *x0, double *x1, hz_solve_info &inf, int &status)
+{
+    cudaStream_t s = op->stream;
+    hz_solver_state *st = solver_of(op);
+    const int64_t n = op->n;
+    HZ_TRY(st->vec.ensure((size_t)n * sizeof(double) * 4));
+    HZ_TRY(st->small.ensure(vec_partial_bytes() + 64));
+    double *r0 = st->vec.as<double>(), *r1 = r0 + n, *q0 = r0 + 2 * n, *q1 = r0 + 3 * n;
+    int iters = 0;
+    status = HZ_OK;
+    double resid = 0.0;
+    if (o.precision != HZ_PREC_F32_REFINED && o.method == HZ_GMRES) {
+        MatrixFreeOp Af(op, o.precision);
+        AdjointOp Aa(Af);
+        LinOp &A = adjoint ? static_cast<LinOp &>(Aa) : static_cast<LinOp &>(Af);
+        int products = 0;
+        HZ_TRY(gmres_solve(A, n, o.restart, b0, b1, x0, x1, o.tol, o.maxit, 0, st->gwork, st->gsmall, s, iters,
+                           resid, products));
+        inf.iterations = iters;
+        inf.resid = resid;
+        inf.resid_f64 = (o.precision == HZ_PREC_F64) ? resid : -1.0;
+        inf.pair_evals = (long long)products * n * n;
+        return HZ_OK;
+    }
+    if (o.precision != HZ_PREC_F32_REFINED) {
+        HZ_TRY(st->outer.reserve(n));
+        MatrixFreeOp Af(op, o.precision);
+        AdjointOp Aa(Af);
+        LinOp &A = adjoint ? static_cast<LinOp &>(Aa) : static_cast<LinOp &>(Af);
+        HZ_TRY(st->outer.solve(A, o.method, b0, b1, o.tol, o.maxit, o.stagnation != 0, true, s, iters, resid, status));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(x0, st->outer.re(Krylov::X), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(x1, st->outer.im(Krylov::X), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        inf.iterations = iters;
+        inf.resid = resid;
+        inf.resid_f64 = (o.precision == HZ_PREC_F64) ? resid : -1.0;
+        // two matrix products per iteration (A p and A^H pt, or two A products)
+        inf.pair_evals = 2LL * iters * n * n;
+        return HZ_OK;
+    }
+    // FP64 iterative refinement around FP32 inner solves.
+    HZ_TRY(st->inner.reserve(n));
+    MatrixFreeOp A32f(op, HZ_PREC_F32), A64f(op, HZ_PREC_F64);
+    AdjointOp A32a(A32f), A64a(A64f);
+    LinOp &A32 = adjoint ? static_cast<LinOp &>(A32a) : static_cast<LinOp &>(A32f);
+    LinOp &A64 = adjoint ? static_cast<LinOp &>(A64a) : static_cast<LinOp &>(A64f);
+    double *part = st->small.as<double>();
+    double *dout = part + (vec_partial_bytes() / sizeof(double));
+    double normb = 0.0, nr = 0.0;
+    HZ_TRY(vec_norm(n, b0, b1, part, dout, normb, s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(x0, 0, n * sizeof(double), s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(x1, 0, n * sizeof(double), s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(r0, b0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(r1, b1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    nr = normb;
+    double res = (normb > 0) ? 1.0 : 0.0;
+    int outer = 0;
+    long long products = 0;
+    const bool gm = o.method == HZ_GMRES;
+    if (gm) HZ_TRY(st->gx.ensure((size_t)n * 2 * sizeof(double)));
+    while (normb > 0 && res >= o.tol && outer < o.max_outer) {
+        outer++;
+        // inner right-hand side r / ||r|| (into q)
+        HZ_TRY(vec_scale(n, 1.0 / nr, r0, r1, q0, q1, s));
+        int it = 0, ist = HZ_OK;
+        double ires = 0.0;
+        const double *e0, *e1;
+        if (gm) {
+            int prods = 0;
+            double *g0 = st->gx.as<double>(), *g1 = g0 + n;
+            HZ_TRY(gmres_solve(A32, n, o.restart, q0, q1, g0, g1, o.inner_tol, o.maxit, kInnerStall, st->gwork,
+                               st->gsmall, s, it, ires, prods));
+            products += prods;
+            e0 = g0;
+            e1 = g1;
+        } else {
+            HZ_TRY(st->inner.solve(A32, o.method, q0, q1, o.inner_tol, o.maxit, o.stagnation != 0, true, s, it, ires,
+                                   ist, kInnerStall));
+            products += 2LL * it;
+            e0 = st->inner.re(Krylov::X);
+            e1 = st->inner.im(Krylov::X);
+        }
+        iters += it;
+        if (ist != HZ_OK && ist != HZ_ERR_BREAKDOWN) {
+            status = ist;
+            break;
+        }
+        HZ_TRY(vec_axpy(n, nr, e0, e1, x0, x1, s));
+        // r = b - A x with the FP64 sweep
+        HZ_TRY(A64.apply(SWEEP_A, x0, x1, nullptr, nullptr, q0, q1, nullptr, nullptr, s));
+        HZ_TRY(vec_sub(n, b0, b1, q0, q1, r0, r1, s));
+        HZ_TRY(vec_norm(n, r0, r1, part, dout, nr, s));
+        A64.iteration_done(false);
+        const double prev = res;
+        res = nr / normb;
+        if (ist == HZ_ERR_BREAKDOWN && !(res < prev)) {
+            status = HZ_ERR_BREAKDOWN;
+            break;
+        }
+    }
+    inf.iterations = iters;
+    inf.outer = outer;
+    inf.resid = res;
+    inf.resid_f64 = res;
+    // inner products (two per BiCG iteration); one FP64 residual product per step
+    inf.pair_evals = (products + outer) * (long long)n * n;
+    return HZ_OK;
+}
+
+static int check_opts(const hz_solve_opts &o)
+{
+    if (o.method != HZ_BICG && o.method != HZ_BICGSTAB && o.method != HZ_GMRES) {
+        set_error("unknown method %d", o.method);
+        return HZ_ERR_ARG;
+    }
+    if (o.precision < HZ_PREC_F64 || o.precision > HZ_PREC_F32_REFINED || !(o.tol > 0) || o.maxit < 1 ||
+        (o.method == HZ_GMRES && (o.restart < 2 || o.restart > 127))) {
+        set_error("bad solve options");
+        return HZ_ERR_ARG;
+    }
     return HZ_OK;
 }
 
@@ -594,17 +981,9 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
     hz_solve_opts o;
     if (opts_in) o = *opts_in;
     else hz_solve_opts_default(&o);
-    if (o.method != HZ_BICG && o.method != HZ_BICGSTAB) {
-        set_error("unknown method %d", o.method);
-        return HZ_ERR_ARG;
-    }
-    if (o.precision < HZ_PREC_F64 || o.precision > HZ_PREC_F32_REFINED || !(o.tol > 0) || o.maxit < 1) {
-        set_error("bad solve options");
-        return HZ_ERR_ARG;
-    }
+    HZ_TRY(check_opts(o));
     HZ_CHECK_CUDA(cudaSetDevice(op->device));
     cudaStream_t s = op->stream;
-    hz_solver_state *st = solver_of(op);
     const int64_t n = op->n;
     hz_solve_info inf{};
     auto t0 = std::chrono::steady_clock::now();
@@ -612,77 +991,16 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
         if (info) *info = inf;
         return HZ_OK;
     }
-    HZ_TRY(st->vec.ensure((size_t)n * sizeof(double) * 8));
-    HZ_TRY(st->small.ensure(vec_partial_bytes() + 64));
-    double *b0 = st->vec.as<double>();
-    double *b1 = b0 + n, *x0 = b0 + 2 * n, *x1 = b0 + 3 * n, *r0 = b0 + 4 * n, *r1 = b0 + 5 * n, *q0 = b0 + 6 * n,
-           *q1 = b0 + 7 * n;
+    // b and x staging: the operator's io buffer (8 n doubles)
+    double *io = op->io.as<double>();
+    double *b0 = io, *b1 = io + n, *x0 = io + 2 * n, *x1 = io + 3 * n;
     HZ_TRY(stage_in(b0, b_re, n, where, s));
     HZ_TRY(stage_in(b1, b_im, n, where, s));
     HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
-    int iters = 0, status = HZ_OK;
-    double resid = 0.0;
-    if (o.precision != HZ_PREC_F32_REFINED) {
-        HZ_TRY(st->outer.reserve(n));
-        MatrixFreeOp A(op, o.precision);
-        HZ_TRY(st->outer.solve(A, o.method, b0, b1, o.tol, o.maxit, o.stagnation != 0, true, s, iters, resid, status));
-        HZ_TRY(stage_out(x_re, st->outer.re(Krylov::X), n, where, s));
-        HZ_TRY(stage_out(x_im, st->outer.im(Krylov::X), n, where, s));
-        inf.iterations = iters;
-        inf.resid = resid;
-        inf.resid_f64 = (o.precision == HZ_PREC_F64) ? resid : -1.0;
-        // two matrix products per iteration (A p and A^H pt, or two A products)
-        inf.pair_evals = 2LL * iters * n * n;
-    } else {
-        // FP64 iterative refinement around FP32 inner solves.
-        HZ_TRY(st->inner.reserve(n));
-        MatrixFreeOp A32(op, HZ_PREC_F32), A64(op, HZ_PREC_F64);
-        double *part = st->small.as<double>();
-        double *dout = part + (vec_partial_bytes() / sizeof(double));
-        double normb = 0.0, nr = 0.0;
-        HZ_TRY(vec_norm(n, b0, b1, part, dout, normb, s));
-        HZ_CHECK_CUDA(cudaMemsetAsync(x0, 0, n * sizeof(double), s));
-        HZ_CHECK_CUDA(cudaMemsetAsync(x1, 0, n * sizeof(double), s));
-        HZ_CHECK_CUDA(cudaMemcpyAsync(r0, b0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        HZ_CHECK_CUDA(cudaMemcpyAsync(r1, b1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        nr = normb;
-        double res = (normb > 0) ? 1.0 : 0.0;
-        int outer = 0;
-        while (normb > 0 && res >= o.tol && outer < o.max_outer) {
-            outer++;
-            // inner right-hand side r / ||r|| (into q)
-            HZ_TRY(vec_scale(n, 1.0 / nr, r0, r1, q0, q1, s));
-            int it = 0, ist = HZ_OK;
-            double ires = 0.0;
-            HZ_TRY(st->inner.solve(A32, o.method, q0, q1, o.inner_tol, o.maxit, o.stagnation != 0, true, s, it, ires,
-                                   ist));
-            iters += it;
-            if (ist != HZ_OK && ist != HZ_ERR_BREAKDOWN) {
-                status = ist;
-                break;
-            }
-            HZ_TRY(vec_axpy(n, nr, st->inner.re(Krylov::X), st->inner.im(Krylov::X), x0, x1, s));
-            // r = b - A x with the FP64 sweep
-            HZ_TRY(A64.apply(SWEEP_A, x0, x1, nullptr, nullptr, q0, q1, nullptr, nullptr, s));
-            HZ_TRY(vec_sub(n, b0, b1, q0, q1, r0, r1, s));
-            HZ_TRY(vec_norm(n, r0, r1, part, dout, nr, s));
-            A64.iteration_done(false);
-            const double prev = res;
-            res = nr / normb;
-            if (ist == HZ_ERR_BREAKDOWN && !(res < prev)) {
-                status = HZ_ERR_BREAKDOWN;
-                break;
-            }
-        }
-        HZ_TRY(stage_out(x_re, x0, n, where, s));
-        HZ_TRY(stage_out(x_im, x1, n, where, s));
-        inf.iterations = iters;
-        inf.outer = outer;
-        inf.resid = res;
-        inf.resid_f64 = res;
-        // inner iterations: two products each; one FP64 residual product per step
-        inf.pair_evals = 2LL * iters * n * n + (long long)outer * n * n;
-    }
+    int status = HZ_OK;
+    HZ_TRY(solve_device(op, o, false, b0, b1, x0, x1, inf, status));
+    HZ_TRY(stage_out(x_re, x0, n, where, s));
+    HZ_TRY(stage_out(x_im, x1, n, where, s));
     HZ_CHECK_CUDA(cudaStreamSynchronize(s));
     int rc = check_device_error(op, "hz_solve");
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
@@ -692,6 +1010,113 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
     if (status != HZ_OK) {
         set_error("solver stopped early (status %d)", status);
         return status;
+    }
+    return HZ_OK;
+}
+
+int hz_misfit_gradient(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, const double *b_im,
+                       int layer, int64_t m, const double *rx, const double *t_re, const double *t_im, double *J,
+                       double *g_re, double *g_im, double *dJ_dk, double *dJ_dw, int where, hz_solve_info *info)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    hz_solve_opts o;
+    if (opts_in) o = *opts_in;
+    else hz_solve_opts_default(&o);
+    HZ_TRY(check_opts(o));
+    if (m < 1 || !rx || !t_re || !t_im || (layer != HZ_SINGLE_LAYER && layer != HZ_DOUBLE_LAYER)) {
+        set_error("hz_misfit_gradient: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    const int64_t n = op->n;
+    auto t0 = std::chrono::steady_clock::now();
+    // device layout: b, sigma, lambda, s, dA sigma (re/im, n each); receivers
+    // (3m), targets, u, r, dE sigma (re/im, m each)
+    DevBuf buf;
+    HZ_TRY(buf.ensure((10 * (size_t)n + 11 * (size_t)m) * sizeof(double)));
+    double *b0 = buf.as<double>(), *b1 = b0 + n, *sg0 = b0 + 2 * n, *sg1 = b0 + 3 * n, *l0 = b0 + 4 * n,
+           *l1 = b0 + 5 * n, *s0 = b0 + 6 * n, *s1 = b0 + 7 * n, *d0 = b0 + 8 * n, *d1 = b0 + 9 * n;
+    double *R = b0 + 10 * n, *T0 = R + 3 * m, *T1 = T0 + m, *U0 = T1 + m, *U1 = U0 + m, *E0 = U1 + m, *E1 = E0 + m,
+           *Q0 = E1 + m, *Q1 = Q0 + m;
+    HZ_TRY(stage_in(b0, b_re, n, where, s));
+    HZ_TRY(stage_in(b1, b_im, n, where, s));
+    HZ_TRY(stage_in(R, rx, 3 * m, where, s));
+    HZ_TRY(stage_in(T0, t_re, m, where, s));
+    HZ_TRY(stage_in(T1, t_im, m, where, s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    hz_solve_info fwd{}, adj{};
+    int status = HZ_OK, status2 = HZ_OK;
+    // forward: A sigma = b, u = E sigma, residual r = u - t
+    HZ_TRY(solve_device(op, o, false, b0, b1, sg0, sg1, fwd, status));
+    HZ_TRY(launch_eval(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), sg0, sg1, m, R, op->p.wave, op->tau,
+                       op->p.interior, layer, U0, U1, s));
+    HZ_TRY(vec_sub(m, U0, U1, T0, T1, E0, E1, s));  // E := r
+    // adjoint: A^H lambda = E^H r
+    HZ_TRY(launch_eval_adjoint(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), m, R, E0, E1, op->p.wave,
+                               op->tau, op->p.interior, layer, s0, s1, s));
+    HZ_TRY(solve_device(op, o, true, s0, s1, l0, l1, adj, status2));
+    // k-derivatives: (dE/dk) sigma at the receivers, (dA/dk) sigma over the tube
+    HZ_TRY(launch_eval_dk(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), sg0, sg1, m, R, op->p.wave,
+                          op->tau, op->p.interior, layer, Q0, Q1, s));
+    HZ_TRY(launch_sweep_dk(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->dreg.as<double>(), sg0,
+                           sg1, op->p.wave, op->tau, op->p.interior, op->p.dirichlet, d0, d1, s));
+    // host side of the small reductions
+    std::vector<double> hr0(m), hr1(m), hq0(m), hq1(m);
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hr0.data(), E0, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hr1.data(), E1, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hq0.data(), Q0, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hq1.data(), Q1, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    std::vector<double> hl0(n), hl1(n), hd0(n), hd1(n), hs0(n), hs1(n), hw(n);
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hl0.data(), l0, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hl1.data(), l1, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hd0.data(), d0, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hd1.data(), d1, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hs0.data(), sg0, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hs1.data(), sg1, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hw.data(), op->w.ptr, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    // J = sum |r|^2;  dJ/dk = 2 Re(r^H (dE/dk) sigma) - 2 Re(lambda^H (dA/dk) sigma)
+    double jv = 0.0, dk = 0.0;
+    for (int64_t i = 0; i < m; i++) {
+        jv += hr0[i] * hr0[i] + hr1[i] * hr1[i];
+        dk += 2.0 * (hr0[i] * hq0[i] + hr1[i] * hq1[i]);
+    }
+    for (int64_t i = 0; i < n; i++) dk -= 2.0 * (hl0[i] * hd0[i] + hl1[i] * hd1[i]);
+    if (J) *J = jv;
+    if (dJ_dk) *dJ_dk = dk;
+    // dJ/db = 2 lambda (gradient w.r.t. Re b and Im b)
+    if (g_re || g_im) {
+        HZ_TRY(vec_scale(n, 2.0, l0, l1, s0, s1, s));
+        HZ_TRY(stage_out(g_re, s0, n, where, s));
+        HZ_TRY(stage_out(g_im, s1, n, where, s));
+    }
+    // dJ/dw_s = Re(conj(lambda_s) sigma_s) / w_s  (A = K W + I/2, E = E' W)
+    if (dJ_dw) {
+        std::vector<double> gw(n);
+        for (int64_t i = 0; i < n; i++)
+            gw[i] = hw[i] != 0.0 ? (hl0[i] * hs0[i] + hl1[i] * hs1[i]) / hw[i] : 0.0;
+        if (where == HZ_HOST) memcpy(dJ_dw, gw.data(), n * sizeof(double));
+        else HZ_CHECK_CUDA(cudaMemcpyAsync(dJ_dw, gw.data(), n * sizeof(double), cudaMemcpyHostToDevice, s));
+    }
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    int rc = check_device_error(op, "hz_misfit_gradient");
+    if (info) {
+        hz_solve_info inf = fwd;
+        inf.iterations = fwd.iterations + adj.iterations;
+        inf.outer = fwd.outer + adj.outer;
+        inf.resid = fwd.resid > adj.resid ? fwd.resid : adj.resid;
+        inf.resid_f64 = fwd.resid_f64 > adj.resid_f64 ? fwd.resid_f64 : adj.resid_f64;
+        inf.pair_evals = fwd.pair_evals + adj.pair_evals + n * n;
+        inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        inf.status = rc != HZ_OK ? rc : (status != HZ_OK ? status : status2);
+        *info = inf;
+    }
+    if (rc != HZ_OK) return rc;
+    if (status != HZ_OK || status2 != HZ_OK) {
+        set_error("solver stopped early (status %d / %d)", status, status2);
+        return status != HZ_OK ? status : status2;
     }
     return HZ_OK;
 }
@@ -758,6 +1183,40 @@ int hz_eval(hz_operator *op, int layer, int64_t m, const double *rx, const doubl
     return HZ_OK;
 }
 
+int hz_eval_slice(hz_operator *op, int layer, int axis, double c, int n2, double lo, double h2, double mask,
+                  const double *s_re, const double *s_im, double *u_re, double *u_im, int where)
+{
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    if (axis < 0 || axis > 2 || n2 < 1 || n2 > 16384 || !(h2 > 0) ||
+        (layer != HZ_SINGLE_LAYER && layer != HZ_DOUBLE_LAYER)) {
+        set_error("hz_eval_slice: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    cudaStream_t s = op->stream;
+    const int64_t m = (int64_t)n2 * n2;
+    const size_t n = (size_t)op->n;
+    DevBuf tmp;
+    HZ_TRY(tmp.ensure((3 * (size_t)m + 2 * (size_t)m + 2 * n) * sizeof(double) + (size_t)m + 64));
+    double *rx = tmp.as<double>(), *ur = rx + 3 * m, *ui = ur + m, *sr = ui + m, *si = sr + n;
+    unsigned char *keep = reinterpret_cast<unsigned char *>(si + n);
+    const double *dsr = s_re, *dsi = s_im;
+    if (where == HZ_HOST) {
+        HZ_TRY(stage_in(sr, s_re, n, where, s));
+        HZ_TRY(stage_in(si, s_im, n, where, s));
+        dsr = sr;
+        dsi = si;
+    }
+    HZ_TRY(launch_slice(axis, c, n2, lo, h2, mask, op->p.N, op->H, op->p.int_l, op->d.as<double>(), rx, keep, s));
+    HZ_TRY(launch_eval(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), dsr, dsi, m, rx, op->p.wave,
+                       op->tau, op->p.interior, layer, ur, ui, s));
+    HZ_TRY(launch_mask(m, keep, ur, ui, s));
+    HZ_TRY(stage_out(u_re, ur, m, where, s));
+    HZ_TRY(stage_out(u_im, ui, m, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
 int hz_assign_gradient(int N, double H, const double *d, double *gx, double *gy, double *gz, int weno_order,
                        int where)
 {
@@ -781,6 +1240,27 @@ int hz_assign_gradient(int N, double H, const double *d, double *gx, double *gy,
     HZ_TRY(stage_out(gx, b + nodes, nodes, where, s));
     HZ_TRY(stage_out(gy, b + 2 * nodes, nodes, where, s));
     HZ_TRY(stage_out(gz, b + 3 * nodes, nodes, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+int hz_reinitialize(int N, double H, double *phi, int iters, double cfl, int weno_order, int where)
+{
+    HZ_TRY(where_ok(where));
+    if (N < 8 || !phi || iters < 0 || !(cfl > 0) || cfl > 1.0 || (weno_order != 3 && weno_order != 5)) {
+        set_error("hz_reinitialize: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    const size_t S = (size_t)N + 1, nodes = S * S * S;
+    cudaStream_t s = nullptr;
+    DevBuf buf;
+    HZ_TRY(buf.ensure(4 * nodes * sizeof(double)));
+    double *b = buf.as<double>();
+    double *dphi = b + 3 * nodes;
+    HZ_TRY(stage_in(dphi, phi, nodes, where, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(b, dphi, nodes * sizeof(double), cudaMemcpyDeviceToDevice, s));  // phi0
+    HZ_TRY(launch_reinit(N, H, dphi, b + nodes, b + 2 * nodes, b, iters, cfl, weno_order, s));
+    HZ_TRY(stage_out(phi, dphi, nodes, where, s));
     HZ_CHECK_CUDA(cudaStreamSynchronize(s));
     return HZ_OK;
 }

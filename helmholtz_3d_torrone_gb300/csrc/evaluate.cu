@@ -105,6 +105,75 @@ __global__ void rhs_kernel(int64_t n, const double4_32a *__restrict__ pos, const
     }
 }
 
+// Receivers on a plane and a mask from the trilinearly interpolated
+// distance grid (1 = keep, 0 = inside or within mask of the surface).
+__global__ void slice_points_kernel(int axis, double c, int n2, double lo, double h2, double mask, int N, double H,
+                                    double int_l, const double *__restrict__ d, double *rx, unsigned char *keep)
+{
+    const int64_t total = (int64_t)n2 * n2;
+    const long long S = N + 1;
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < total; q += (int64_t)gridDim.x * blockDim.x) {
+        const int a = (int)(q / n2), b = (int)(q % n2);
+        const double u = lo + a * h2, v = lo + b * h2;
+        double x, y, z;
+        if (axis == 0) { x = c; y = u; z = v; }
+        else if (axis == 1) { x = u; y = c; z = v; }
+        else { x = u; y = v; z = c; }
+        rx[3 * q] = x;
+        rx[3 * q + 1] = y;
+        rx[3 * q + 2] = z;
+        int i = (int)floor((y - int_l) / H), j = (int)floor((x - int_l) / H), k = (int)floor((z - int_l) / H);
+        unsigned char kp = 1;
+        if (i >= 0 && j >= 0 && k >= 0 && i < N && j < N && k < N) {
+            const double ly = (y - int_l) / H - i, lx = (x - int_l) / H - j, lz = (z - int_l) / H - k;
+            const long long o = ((long long)i * S + j) * S + k;
+            double acc = 0.0;
+            for (int di = 0; di < 2; di++)
+                for (int dj = 0; dj < 2; dj++)
+                    for (int dk = 0; dk < 2; dk++) {
+                        const double wgt = (di ? ly : 1 - ly) * (dj ? lx : 1 - lx) * (dk ? lz : 1 - lz);
+                        acc += wgt * d[o + di * S * S + dj * S + dk];
+                    }
+            if (acc > -mask) kp = 0;
+        }
+        keep[q] = kp;
+    }
+}
+
+__global__ void apply_mask_kernel(int64_t m, const unsigned char *__restrict__ keep, double *u_re, double *u_im)
+{
+    for (int64_t q = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; q < m; q += (int64_t)gridDim.x * blockDim.x)
+        if (!keep[q]) {
+            u_re[q] = 0.0;
+            u_im[q] = 0.0;
+        }
+}
+
+// Incident plane waves u = e^{ik d.x} at the projected points, one column
+// [ndir][n] per direction: Dirichlet data (kind 0) or its derivative along
+// the outward normal -n (kind 1).
+__global__ void plane_wave_kernel(int64_t n, const double4_32a *__restrict__ pos, const double4_32a *__restrict__ nrm,
+                                  int ndir, const double *__restrict__ dirs, double W, int kind, double *b_re,
+                                  double *b_im)
+{
+    const int r = blockIdx.y;
+    const double dx = dirs[3 * r], dy = dirs[3 * r + 1], dz = dirs[3 * r + 2];
+    for (int64_t c = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; c < n; c += (int64_t)gridDim.x * blockDim.x) {
+        const double4_32a p = pos[c];
+        double S, C;
+        sincos(W * (dx * p.x + dy * p.y + dz * p.z), &S, &C);
+        double re = C, im = S;
+        if (kind == HZ_RHS_POINT_NEUMANN) {
+            const double4_32a q = nrm[c];
+            const double dn = -(dx * q.x + dy * q.y + dz * q.z);  // d . n_out
+            re = -W * dn * S;                                     // i k (d.n_out) e^{ik d.x}
+            im = W * dn * C;
+        }
+        b_re[(int64_t)r * n + c] = re;
+        b_im[(int64_t)r * n + c] = im;
+    }
+}
+
 // Dense complex products on a row-major n x n matrix (real and imaginary
 // parts), large3Dexample2.c:3262-3309: q = A p and qt = A^H pt in one pass
 // over A.  A block owns kDenseRows rows; each warp walks its rows with
@@ -195,6 +264,37 @@ int launch_rhs(int64_t n, const double4_32a *pos, const double4_32a *nrm, const 
     long long b = (n + 255) / 256;
     if (b > 4096) b = 4096;
     rhs_kernel<<<(unsigned)b, 256, 0, s>>>(n, pos, nrm, src[0], src[1], src[2], wave, kind, b_re, b_im);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
+int launch_plane_waves(int64_t n, const double4_32a *pos, const double4_32a *nrm, int ndir, const double *dirs,
+                       double wave, int kind, double *b_re, double *b_im, cudaStream_t s)
+{
+    if (n <= 0) return HZ_OK;
+    long long b = (n + 255) / 256;
+    if (b > 256) b = 256;
+    plane_wave_kernel<<<dim3((unsigned)b, (unsigned)ndir), 256, 0, s>>>(n, pos, nrm, ndir, dirs, wave, kind, b_re, b_im);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
+int launch_slice(int axis, double c, int n2, double lo, double h2, double mask, int N, double H, double int_l,
+                 const double *d, double *rx, unsigned char *keep, cudaStream_t s)
+{
+    const int64_t total = (int64_t)n2 * n2;
+    long long b = (total + 255) / 256;
+    if (b > 4096) b = 4096;
+    slice_points_kernel<<<(unsigned)b, 256, 0, s>>>(axis, c, n2, lo, h2, mask, N, H, int_l, d, rx, keep);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
+int launch_mask(int64_t m, const unsigned char *keep, double *u_re, double *u_im, cudaStream_t s)
+{
+    long long b = (m + 255) / 256;
+    if (b > 4096) b = 4096;
+    apply_mask_kernel<<<(unsigned)b, 256, 0, s>>>(m, keep, u_re, u_im);
     HZ_CHECK_LAUNCH();
     return HZ_OK;
 }

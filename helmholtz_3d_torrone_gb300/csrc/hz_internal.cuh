@@ -84,7 +84,7 @@ struct Rec32 {
     int *perm;           // npad entries, -1 for padding
     float4 *pos;         // x-o, y-o, z-o relative to the slot's tile origin; .w = reg
     float4 *nrm;         // nx, ny, nz, w
-    double4_32a *origin;     // per tile: origin (x, y, z), unused
+    double4_32a *origin;     // per tile: origin (x, y, z) and bounding radius .w
     double4_32a *tpos;       // per slot FP64 position (x, y, z), .w = w (targets)
 };
 
@@ -118,18 +118,24 @@ struct SweepTimer {
 // stencils.cu
 int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
                          double *mc, double *gc, int order, cudaStream_t s);
+// reinitialisation (stencils.cu): iters TVD-RK2 steps of dt = cfl*H, in place
+int launch_reinit(int N, double H, double *phi, double *tmp1, double *tmp2, const double *phi0, int iters,
+                  double cfl, int order, cudaStream_t s);
 // tube.cu
 int tube_build(int N, double eps, const double *d, DevBuf &idx, int64_t &n, DevBuf &scratch,
                cudaStream_t s);
 int tube_init(const hz_params &p, const double *d, const double *gx, const double *gy,
               const double *gz, const double *mc, const double *gc, int64_t n, const int64_t *idx,
               double *xs, double *nrm, double *delta, double *jac, double *reg, double *w,
-              double4_32a *pos64, double4_32a *nrm64, unsigned *err, cudaStream_t s);
+              double4_32a *pos64, double4_32a *nrm64, unsigned *err, cudaStream_t s,
+              double *dreg = nullptr);
 int sweep_order(int N, int64_t n, const int64_t *idx, int *perm, int64_t npad, DevBuf &scratch,
                 cudaStream_t s);
+// reg_scale multiplies the regularisation factor stored in pos32.w (the
+// FP32 sweep folds sg/(4 pi) into its densities and divides it out here).
 int build_rec32(int64_t n, int64_t npad, const int *perm, const double4_32a *pos64,
                 const double4_32a *nrm64, float4 *pos32, float4 *nrm32, double4_32a *origin,
-                double4_32a *tpos, cudaStream_t s);
+                double4_32a *tpos, double reg_scale, cudaStream_t s);
 // sweep_f64.cu
 int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re, const double *p_im,
               const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
@@ -139,7 +145,11 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode,
               const double *p_re, const double *p_im, const double *pt_re, const double *pt_im,
               double *q_re, double *q_im, double *qt_re, double *qt_im, float4 *dens,
-              cudaStream_t s, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
+              cudaStream_t s, cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr, int cfg = 0);
+// 1 / (sg / 4 pi): the factor applied to regularisation factors in pos32.w
+double sweep32_reg_scale(int interior);
+// number of compiled FP32 sweep variants (block shape x targets per thread)
+int sweep32_num_configs();
 
 }  // namespace hz
 
@@ -157,7 +167,7 @@ struct hz_operator {
     bool have_distance = false, built = false;
     // tube
     int64_t n = 0;
-    hz::DevBuf idx, xs, nrm, delta, jac, reg, w;
+    hz::DevBuf idx, xs, nrm, delta, jac, reg, w, dreg;
     hz::DevBuf pos64, nrm64;
     // FP32 sweep records
     hz::Rec32 r32{};
@@ -168,6 +178,7 @@ struct hz_operator {
     hz::DevBuf dens32;
     hz_solver_state *solver = nullptr;  // Krylov workspaces (capi.cu)
     hz::SweepTimer timer;
+    int sweep_cfg = 0;  // FP32 sweep variant (hz_autotune)
 };
 
 namespace hz {

@@ -369,7 +369,9 @@ int Krylov::reserve(int64_t n_)
 {
     n = n_;
     const size_t vec = (size_t)n * sizeof(double);
+    void *before = vecs.ptr;
     HZ_TRY(vecs.ensure(vec * 2 * kVecs));
+    if (vecs.ptr != before) invalidate_graph();  // the graph holds the old vectors
     HZ_TRY(partial.ensure((size_t)kDotBlocks * kMaxDots * sizeof(double) * 2));
     HZ_TRY(scal.ensure(sizeof(KrylovScalars)));
     if (!host_err) HZ_CHECK_CUDA(cudaMallocHost(&host_err, 4 * sizeof(double)));
@@ -435,7 +437,7 @@ int Krylov::stab_iteration(LinOp &A, cudaStream_t s)
 }
 
 int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, double tol, int maxit,
-                  bool stagnation, bool use_graph, cudaStream_t s, int &iters, double &resid, int &status)
+                  bool stagnation, bool use_graph, cudaStream_t s, int &iters, double &resid, int &status, int stall)
 {
     double *pp = partial.as<double>();
     KrylovScalars *sc = scal.as<KrylovScalars>();
@@ -471,7 +473,7 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
     // stream changes; the graph is keyed by method and operator)
     cudaGraphExec_t exec = nullptr;
     if (use_graph) {
-        if (graph_exec && graph_key_op == &A && graph_key_method == method && graph_stream == s) {
+        if (graph_exec && graph_key != 0 && graph_key == A.key() && graph_key_method == method && graph_stream == s) {
             exec = graph_exec;
         } else {
             if (graph_exec) {
@@ -493,7 +495,7 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
             }
             cudaGetLastError();
             if (captured) {
-                graph_key_op = &A;
+                graph_key = A.key();
                 graph_key_method = method;
                 graph_stream = s;
                 exec = graph_exec;
@@ -502,7 +504,8 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
             }
         }
     }
-    double err = 1.0;
+    double err = 1.0, best = 1e300;
+    int best_it = 0;
     for (int it = 1; it <= maxit; it++) {
         if (exec) {
             HZ_CHECK_CUDA(cudaGraphLaunch(exec, s));
@@ -526,6 +529,12 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
             break;
         }
         if (stagnation && fabs(preerr - err) < 1e-3 * tol) break;
+        if (err < best) {
+            best = err;
+            best_it = it;
+        } else if (stall > 0 && it - best_it >= stall) {
+            break;
+        }
     }
     resid = err;
     return HZ_OK;

@@ -1,0 +1,42 @@
+// krylov_multi.cuh -- lockstep BiCGSTAB over R right-hand sides.
+#pragma once
+
+#include <vector>
+
+#include "hz_internal.cuh"
+
+namespace hz {
+
+// Q = A P for R column vectors stored one after the other ([R][n]).
+struct MultiOp {
+    virtual ~MultiOp() = default;
+    virtual int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im,
+                      cudaStream_t s) = 0;
+};
+
+class KrylovMulti {
+  public:
+    enum { X = 0, RV, RH, P, V, T, kVecs };
+    ~KrylovMulti();
+    int reserve(int64_t n, int R);
+    // Solve A X = B column by column (x0 = 0); B on the device, [R][n].
+    int solve(MultiOp &A, const double *b_re, const double *b_im, double tol, int maxit, bool stagnation,
+              cudaStream_t s, int &iters, std::vector<double> &resid, int stall = 0);
+    double *re(int v);
+    double *im(int v);
+
+  private:
+    int64_t n = 0;
+    int R = 0;
+    DevBuf vecs, partial, scal;
+    double *host = nullptr;
+};
+
+// sweep_multi.cu
+int multi_rhs_block();
+size_t multi_rhs_scratch_bytes(int64_t n, int64_t npad);
+int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int precision, int nrhs,
+                const double *p_re, const double *p_im, double *q_re, double *q_im, void *scratch,
+                cudaStream_t s);
+
+}  // namespace hz

@@ -228,7 +228,74 @@ __global__ void __launch_bounds__(256) grid_kernel(int N, double H, const double
     }
 }
 
+// finite_difference3D.c:5-27: Godunov upwind |grad phi| from one-sided
+// derivatives a = D+x, b = D-x, c = D+y, d = D-y, e = D+z, f = D-z.
+__device__ double godunov(double signage, double a, double b, double c, double d, double e, double f)
+{
+    const double aplus = rmax(a, 0.0) * rmax(a, 0.0), aminus = rmin(a, 0.0) * rmin(a, 0.0);
+    const double bplus = rmax(b, 0.0) * rmax(b, 0.0), bminus = rmin(b, 0.0) * rmin(b, 0.0);
+    const double cplus = rmax(c, 0.0) * rmax(c, 0.0), cminus = rmin(c, 0.0) * rmin(c, 0.0);
+    const double dplus = rmax(d, 0.0) * rmax(d, 0.0), dminus = rmin(d, 0.0) * rmin(d, 0.0);
+    const double eplus = rmax(e, 0.0) * rmax(e, 0.0), eminus = rmin(e, 0.0) * rmin(e, 0.0);
+    const double fplus = rmax(f, 0.0) * rmax(f, 0.0), fminus = rmin(f, 0.0) * rmin(f, 0.0);
+    if (signage > 0) return sqrt(rmax(aminus, bplus) + rmax(cminus, dplus) + rmax(eminus, fplus));
+    if (signage < 0) return sqrt(rmax(aplus, bminus) + rmax(cplus, dminus) + rmax(eplus, fminus));
+    return 0.0;
+}
+
+// One forward-Euler stage of phi_t + S(phi0) (|grad phi| - 1) = 0:
+//   out = base*w0 + (phi - dt S(phi0) (G(phi) - 1))*w1,
+// S(phi0) = phi0 / sqrt(phi0^2 + H^2), G the Godunov Hamiltonian on WENO
+// one-sided derivatives (weno.c:259-345, mirror boundaries).  Two stages
+// with (w0, w1) = (0, 1) then (1/2, 1/2) make the TVD Runge-Kutta 2 step.
+__global__ void __launch_bounds__(256) reinit_stage_kernel(int N, double H, double dt, const double *__restrict__ phi0,
+                                                           const double *__restrict__ phi, const double *__restrict__ base,
+                                                           double w0, double w1, double *__restrict__ out, int order)
+{
+    const long long S = N + 1;
+    const long long total = S * S * S;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
+         o += (long long)gridDim.x * blockDim.x) {
+        const int k = (int)(o % S);
+        const int j = (int)((o / S) % S);
+        const int i = (int)(o / (S * S));
+        const int half = (order == 5) ? 3 : 2;
+        double f[7], Dxp, Dxn, Dyp, Dyn, Dzp, Dzn;
+        for (int m = -half; m <= half; m++) f[m + half] = __ldg(phi + (i * S + mirror(j + m, N)) * S + k);
+        weno(&Dxp, &Dxn, f, H, order);
+        for (int m = -half; m <= half; m++) f[m + half] = __ldg(phi + (mirror(i + m, N) * S + j) * S + k);
+        weno(&Dyp, &Dyn, f, H, order);
+        for (int m = -half; m <= half; m++) f[m + half] = __ldg(phi + (i * S + j) * S + mirror(k + m, N));
+        weno(&Dzp, &Dzn, f, H, order);
+        const double p0 = phi0[o];
+        const double sgn = p0 / sqrt(p0 * p0 + H * H);
+        const double g = godunov(p0, Dxp, Dxn, Dyp, Dyn, Dzp, Dzn);
+        const double stage = phi[o] - dt * sgn * (g - 1.0);
+        out[o] = (w0 != 0.0) ? (w0 * base[o] + w1 * stage) : stage;
+    }
+}
+
 }  // namespace
+
+int launch_reinit(int N, double H, double *phi, double *tmp1, double *tmp2, const double *phi0, int iters,
+                  double cfl, int order, cudaStream_t s)
+{
+    const long long S = N + 1, total = S * S * S;
+    int sms = 152, dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    long long blocks = (total + 255) / 256;
+    if (blocks > (long long)sms * 16) blocks = (long long)sms * 16;
+    const double dt = cfl * H;
+    for (int it = 0; it < iters; it++) {
+        reinit_stage_kernel<<<(unsigned)blocks, 256, 0, s>>>(N, H, dt, phi0, phi, phi, 0.0, 1.0, tmp1, order);
+        HZ_CHECK_LAUNCH();
+        reinit_stage_kernel<<<(unsigned)blocks, 256, 0, s>>>(N, H, dt, phi0, tmp1, phi, 0.5, 0.5, tmp2, order);
+        HZ_CHECK_LAUNCH();
+        HZ_CHECK_CUDA(cudaMemcpyAsync(phi, tmp2, total * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    }
+    return HZ_OK;
+}
 
 int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
                          double *mc, double *gc, int order, cudaStream_t s)

@@ -15,19 +15,30 @@
 //    sweep's own arithmetic) whenever the FP32 rho^2 lies within 1e-4 of
 //    tau^2, so FP32 and FP64 operators classify every pair alike.
 //  * Per tile the contributions are summed in FP32, across tiles in FP64.
-// Each thread owns kTgt32 targets; TMA bulk copies stage source tiles in
-// shared memory, double-buffered on mbarriers with bounded waits.
+//
+// Throughput design: the kernel is bound by instruction issue on the FP32
+// pipe.  A source tile whose bounding sphere is farther than tau (with a
+// 1e-3 margin) from the bounding spheres of all of the block's targets
+// holds no near pair, and runs a loop without near-field tests or selects;
+// only the few tiles next to the block's targets take the full loop.  The
+// factor sg/(4 pi) is folded into the densities (and divided out of the
+// stored regularisation factors).  TMA bulk copies stage source tiles in
+// shared memory, double-buffered on mbarriers with bounded waits.  Block
+// shape and targets per thread come from a small table of compiled
+// variants; the autotuner times them on the operator's own data.
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
 
 namespace hz {
 namespace {
 
+constexpr double kPi = 3.14159265358979323846264338328;
+
 struct Args32 {
     int64_t n, npad;
-    float wave, kh, kl, scale;  // scale = sg / (4 pi)
+    float wave, kh, kl;
     float tau2, guard_lo, guard_hi;
-    double tau;
+    double tau, tau_far;
     const float4 *pos, *nrm, *dens;
     const double4_32a *origin, *tpos;
     const int *perm;
@@ -37,34 +48,92 @@ struct Args32 {
     unsigned *err;
 };
 
-// dens[s] = (w p, pt) at sweep slot s, FP32.
-__global__ void prep32_kernel(int64_t npad, const int *__restrict__ perm, const float4 *__restrict__ nrm,
-                              const double4_32a *__restrict__ tpos, const double *__restrict__ p_re,
-                              const double *__restrict__ p_im, const double *__restrict__ pt_re,
-                              const double *__restrict__ pt_im, float4 *__restrict__ dens)
+// dens[s] = scale (w p, pt) at sweep slot s, FP32, scale = sg / (4 pi).
+__global__ void prep32_kernel(int64_t npad, const int *__restrict__ perm, const double4_32a *__restrict__ tpos,
+                              const double *__restrict__ p_re, const double *__restrict__ p_im,
+                              const double *__restrict__ pt_re, const double *__restrict__ pt_im, double scale,
+                              float4 *__restrict__ dens)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < npad; s += (int64_t)gridDim.x * blockDim.x) {
         const int c = perm[s];
         float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
         if (c >= 0) {
-            const double w = tpos[s].w;
+            const double ws = tpos[s].w * scale;
             if (p_re) {
-                v.x = (float)(w * p_re[c]);
-                v.y = (float)(w * p_im[c]);
+                v.x = (float)(ws * p_re[c]);
+                v.y = (float)(ws * p_im[c]);
             }
             if (pt_re) {
-                v.z = (float)pt_re[c];
-                v.w = (float)pt_im[c];
+                v.z = (float)(scale * pt_re[c]);
+                v.w = (float)(scale * pt_im[c]);
             }
         }
         dens[s] = v;
     }
 }
 
-template <int MODE, bool DIR>
-__global__ void __launch_bounds__(kThreads32, 2) sweep32_kernel(Args32 a)
+// One source against TG targets; NEAR selects the loop with near-field
+// handling.  Accumulates into fA (A p) and fH (A^H pt).
+template <int MODE, bool DIR, int TG, bool NEAR>
+__device__ __forceinline__ void pair_block(const Args32 &a, const float4 s_p, const float4 s_n, const float4 s_d,
+                                           const float3 (&rel)[TG], const float3 (&tn)[TG], const float (&treg)[TG],
+                                           const double4_32a (&tp)[TG], int64_t src_slot, float (&fAr)[TG],
+                                           float (&fAi)[TG], float (&fHr)[TG], float (&fHi)[TG])
 {
-    constexpr int TS = kTile32, NT = kThreads32, TG = kTgt32;
+#pragma unroll
+    for (int g = 0; g < TG; g++) {
+        const float dx = rel[g].x - s_p.x, dy = rel[g].y - s_p.y, dz = rel[g].z - s_p.z;
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        bool near = false;
+        if (NEAR) {
+            near = r2 <= a.tau2;
+            if (r2 > a.guard_lo && r2 < a.guard_hi) {
+                // decide exactly as the FP64 sweep does
+                const int c = a.perm[src_slot];
+                if (c >= 0) {
+                    const double4_32a q = a.pos64[c];
+                    const double x1 = tp[g].x - q.x, x2 = tp[g].y - q.y, x3 = tp[g].z - q.z;
+                    near = !(sqrt(x1 * x1 + x2 * x2 + x3 * x3) > a.tau);
+                }
+            }
+        }
+        const float rinv = rsqrtf(r2);
+        const float rho = r2 * rinv;
+        const float nn = rintf(rho * a.kh);
+        float f = fmaf(rho, a.kh, -nn);
+        f = fmaf(rho, a.kl, f);
+        float S, C;
+        __sincosf(f * 6.28318530717958647692f, &S, &C);
+        const float u1 = fmaf(C, rinv, a.wave * S);   // k sin + cos/rho
+        const float u2 = fmaf(a.wave, C, -S * rinv);  // k cos - sin/rho
+        const float rr = rinv * rinv;
+        const float a1 = -u1 * rr, a2 = u2 * rr;
+        const float pn = dx * s_n.x + dy * s_n.y + dz * s_n.z;        // (x_t-x_s).n_s
+        const float pt = dx * tn[g].x + dy * tn[g].y + dz * tn[g].z;  // (x_t-x_s).n_t
+        const float pA = DIR ? pn : pt, pH = DIR ? pt : pn;
+        float vAr = a1 * pA, vAi = a2 * pA, vHr = -a1 * pH, vHi = a2 * pH;
+        if (NEAR && near) {
+            vAr = DIR ? s_p.w : treg[g];
+            vHr = DIR ? treg[g] : s_p.w;
+            vAi = 0.f;
+            vHi = 0.f;
+        }
+        if (MODE & SWEEP_A) {
+            fAr[g] = fmaf(vAr, s_d.x, fmaf(-vAi, s_d.y, fAr[g]));
+            fAi[g] = fmaf(vAr, s_d.y, fmaf(vAi, s_d.x, fAi[g]));
+        }
+        if (MODE & SWEEP_AH) {
+            fHr[g] = fmaf(vHr, s_d.z, fmaf(-vHi, s_d.w, fHr[g]));
+            fHi[g] = fmaf(vHr, s_d.w, fmaf(vHi, s_d.z, fHi[g]));
+        }
+    }
+}
+
+template <int MODE, bool DIR, int NT, int TG, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
+{
+    constexpr int TS = kTile32;
+    constexpr int NTT = (NT * TG + TS - 1) / TS;  // target tiles per block
     __shared__ alignas(128) float4 sp[2][TS];
     __shared__ alignas(128) float4 sn[2][TS];
     __shared__ alignas(128) float4 sd[2][TS];
@@ -84,6 +153,12 @@ __global__ void __launch_bounds__(kThreads32, 2) sweep32_kernel(Args32 a)
         treg[g] = a.pos[s].w;
         accAr[g] = accAi[g] = accHr[g] = accHi[g] = 0.0;
     }
+    // bounding spheres of the block's targets (block-uniform)
+    double4_32a tsph[NTT];
+    const int64_t ttile0 = ((int64_t)blockIdx.x * NT * TG) / TS;
+#pragma unroll
+    for (int k = 0; k < NTT; k++) tsph[k] = a.origin[ttile0 + k];
+
     const int64_t ntiles = a.npad / TS;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -104,6 +179,12 @@ __global__ void __launch_bounds__(kThreads32, 2) sweep32_kernel(Args32 a)
         const int buf = (int)(tile & 1);
         if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
         const double4_32a o = a.origin[tile];
+        bool far = true;
+#pragma unroll
+        for (int k = 0; k < NTT; k++) {
+            const double ex = o.x - tsph[k].x, ey = o.y - tsph[k].y, ez = o.z - tsph[k].z;
+            far = far && (sqrt(ex * ex + ey * ey + ez * ez) - o.w - tsph[k].w > a.tau_far);
+        }
         float3 rel[TG];
 #pragma unroll
         for (int g = 0; g < TG; g++)
@@ -119,56 +200,17 @@ __global__ void __launch_bounds__(kThreads32, 2) sweep32_kernel(Args32 a)
         float fAr[TG], fAi[TG], fHr[TG], fHi[TG];
 #pragma unroll
         for (int g = 0; g < TG; g++) fAr[g] = fAi[g] = fHr[g] = fHi[g] = 0.f;
+        const int64_t base = tile * TS;
+        if (far) {
 #pragma unroll 2
-        for (int j = 0; j < TS; j++) {
-            const float4 s_p = sp[buf][j];
-            const float4 s_n = sn[buf][j];
-            const float4 s_d = sd[buf][j];
-#pragma unroll
-            for (int g = 0; g < TG; g++) {
-                const float dx = rel[g].x - s_p.x, dy = rel[g].y - s_p.y, dz = rel[g].z - s_p.z;
-                const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-                bool near = r2 <= a.tau2;
-                if (r2 > a.guard_lo && r2 < a.guard_hi) {
-                    // decide exactly as the FP64 sweep does
-                    const int c = a.perm[tile * TS + j];
-                    if (c >= 0) {
-                        const double4_32a q = a.pos64[c];
-                        const double x1 = tp[g].x - q.x, x2 = tp[g].y - q.y, x3 = tp[g].z - q.z;
-                        near = !(sqrt(x1 * x1 + x2 * x2 + x3 * x3) > a.tau);
-                    }
-                }
-                const float rinv = rsqrtf(r2);
-                const float rho = r2 * rinv;
-                const float tt = rho * a.kh;
-                const float nn = rintf(tt);
-                float f = fmaf(rho, a.kh, -nn);
-                f = fmaf(rho, a.kl, f);
-                float S, C;
-                __sincosf(f * 6.28318530717958647692f, &S, &C);
-                const float u1 = fmaf(C, rinv, a.wave * S);   // k sin + cos/rho
-                const float u2 = fmaf(a.wave, C, -S * rinv);  // k cos - sin/rho
-                const float rr = rinv * rinv * a.scale;
-                const float a1 = -u1 * rr, a2 = u2 * rr;
-                const float pn = dx * s_n.x + dy * s_n.y + dz * s_n.z;        // (x_t-x_s).n_s
-                const float pt = dx * tn[g].x + dy * tn[g].y + dz * tn[g].z;  // (x_t-x_s).n_t
-                const float pA = DIR ? pn : pt, pH = DIR ? pt : pn;
-                float vAr = a1 * pA, vAi = a2 * pA, vHr = -a1 * pH, vHi = a2 * pH;
-                if (near) {
-                    vAr = DIR ? s_p.w : treg[g];
-                    vHr = DIR ? treg[g] : s_p.w;
-                    vAi = 0.f;
-                    vHi = 0.f;
-                }
-                if (MODE & SWEEP_A) {
-                    fAr[g] = fmaf(vAr, s_d.x, fmaf(-vAi, s_d.y, fAr[g]));
-                    fAi[g] = fmaf(vAr, s_d.y, fmaf(vAi, s_d.x, fAi[g]));
-                }
-                if (MODE & SWEEP_AH) {
-                    fHr[g] = fmaf(vHr, s_d.z, fmaf(-vHi, s_d.w, fHr[g]));
-                    fHi[g] = fmaf(vHr, s_d.w, fmaf(vHi, s_d.z, fHi[g]));
-                }
-            }
+            for (int j = 0; j < TS; j++)
+                pair_block<MODE, DIR, TG, false>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, tp, base + j,
+                                                 fAr, fAi, fHr, fHi);
+        } else {
+#pragma unroll 2
+            for (int j = 0; j < TS; j++)
+                pair_block<MODE, DIR, TG, true>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, tp, base + j,
+                                                fAr, fAi, fHr, fHi);
         }
 #pragma unroll
         for (int g = 0; g < TG; g++) {
@@ -199,12 +241,33 @@ __global__ void __launch_bounds__(kThreads32, 2) sweep32_kernel(Args32 a)
     }
 }
 
-template <int MODE>
-void launch32(const Args32 &a, bool dir, cudaStream_t s)
+// Compiled variants: block size, targets per thread, minimum resident blocks.
+// Every variant covers 256 or 512 sweep slots per block (npad is a multiple
+// of 512).
+template <int MODE, bool DIR>
+void launch_cfg(int cfg, const Args32 &a, cudaStream_t s)
 {
-    const unsigned blocks = (unsigned)(a.npad / (kThreads32 * kTgt32));
-    if (dir) sweep32_kernel<MODE, true><<<blocks, kThreads32, 0, s>>>(a);
-    else sweep32_kernel<MODE, false><<<blocks, kThreads32, 0, s>>>(a);
+    switch (cfg) {
+    case 1:
+        sweep32_kernel<MODE, DIR, 128, 2, 4><<<(unsigned)(a.npad / 256), 128, 0, s>>>(a);
+        break;
+    case 2:
+        sweep32_kernel<MODE, DIR, 128, 4, 2><<<(unsigned)(a.npad / 512), 128, 0, s>>>(a);
+        break;
+    case 3:
+        sweep32_kernel<MODE, DIR, 256, 1, 3><<<(unsigned)(a.npad / 256), 256, 0, s>>>(a);
+        break;
+    default:
+        sweep32_kernel<MODE, DIR, 256, 2, 2><<<(unsigned)(a.npad / 512), 256, 0, s>>>(a);
+        break;
+    }
+}
+
+template <int MODE>
+void launch32(int cfg, const Args32 &a, bool dir, cudaStream_t s)
+{
+    if (dir) launch_cfg<MODE, true>(cfg, a, s);
+    else launch_cfg<MODE, false>(cfg, a, s);
 }
 
 }  // namespace
@@ -212,7 +275,7 @@ void launch32(const Args32 &a, bool dir, cudaStream_t s)
 // Split k/(2 pi) into a head with 12 significant bits and an FP32 tail.
 void split_wave(double wave, float &kh, float &kl)
 {
-    const double kc = wave / (2.0 * 3.14159265358979323846264338328);
+    const double kc = wave / (2.0 * kPi);
     int e;
     frexp(kc, &e);
     const double q = ldexp(1.0, e - 12);
@@ -221,22 +284,27 @@ void split_wave(double wave, float &kh, float &kl)
     kl = (float)(kc - head);
 }
 
+double sweep32_reg_scale(int interior) { return ((interior == 1) ? -1.0 : 1.0) * (4.0 * kPi); }
+
+int sweep32_num_configs() { return 4; }
+
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode, const double *p_re,
               const double *p_im, const double *pt_re, const double *pt_im, double *q_re, double *q_im,
               double *qt_re, double *qt_im, float4 *dens, cudaStream_t s, cudaEvent_t ev0,
-              cudaEvent_t ev1)
+              cudaEvent_t ev1, int cfg)
 {
     if (c.n <= 0) return HZ_OK;
     const bool useA = (mode & SWEEP_A) != 0, useH = (mode & SWEEP_AH) != 0;
+    const double scale = ((c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi);
     {
         int dev = 0, sms = 152;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         long long b = (r.npad + 255) / 256;
         if (b > sms * 8) b = sms * 8;
-        prep32_kernel<<<(unsigned)b, 256, 0, s>>>(r.npad, r.perm, r.nrm, r.tpos, useA ? p_re : nullptr,
+        prep32_kernel<<<(unsigned)b, 256, 0, s>>>(r.npad, r.perm, r.tpos, useA ? p_re : nullptr,
                                                   useA ? p_im : nullptr, useH ? pt_re : nullptr,
-                                                  useH ? pt_im : nullptr, dens);
+                                                  useH ? pt_im : nullptr, scale, dens);
         HZ_CHECK_LAUNCH();
     }
     Args32 a;
@@ -244,8 +312,8 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.npad = r.npad;
     a.wave = (float)c.wave;
     split_wave(c.wave, a.kh, a.kl);
-    a.scale = (float)(((c.interior == 1) ? -1.0 : 1.0) / (4.0 * 3.14159265358979323846264338328));
     a.tau = c.tau;
+    a.tau_far = c.tau * (1.0 + 1e-3);
     a.tau2 = (float)(c.tau * c.tau);
     a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
     a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
@@ -260,9 +328,9 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
     a.err = c.err;
     if (ev0) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev0, s, cudaEventRecordExternal));
-    if (mode == SWEEP_PAIR) launch32<SWEEP_PAIR>(a, c.dirichlet != 0, s);
-    else if (mode == SWEEP_A) launch32<SWEEP_A>(a, c.dirichlet != 0, s);
-    else launch32<SWEEP_AH>(a, c.dirichlet != 0, s);
+    if (mode == SWEEP_PAIR) launch32<SWEEP_PAIR>(cfg, a, c.dirichlet != 0, s);
+    else if (mode == SWEEP_A) launch32<SWEEP_A>(cfg, a, c.dirichlet != 0, s);
+    else launch32<SWEEP_AH>(cfg, a, c.dirichlet != 0, s);
     HZ_CHECK_LAUNCH();
     if (ev1) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev1, s, cudaEventRecordExternal));
     return HZ_OK;

@@ -12,9 +12,19 @@
 //
 // One thread owns one target; source tiles of kTile64 records (position+reg,
 // normal+weight, prescaled density) are staged in shared memory by TMA bulk
-// copies, double-buffered on mbarriers.  FP64 throughout, following the
-// reference's arithmetic (sqrt, IEEE reciprocal, sincos); the 1/2 diagonal
+// copies, double-buffered on mbarriers.  FP64 throughout; the 1/2 diagonal
 // and the weights are applied in the epilogue.
+//
+// GB300 runs FP64 at about 1/60 of its FP32 rate, so the FP64 arithmetic is
+// kept short: 1/rho comes from rsqrt(rho^2) and rho = rho^2 / rho, and
+// sin/cos use a table-driven method (P. T. P. Tang, "Table-lookup
+// algorithms for elementary functions and their error analysis", 1991):
+// k*rho = m*(2 pi/128) + r with |r| <= pi/128, sin/cos(m 2 pi/128) from a
+// 128-entry shared table, sin/cos(r) from their Taylor series (terms to
+// r^7 and r^6; the first dropped terms are below 1e-20), recombined by the
+// angle-addition formulas.  The near-field decision keeps the reference's
+// test sqrt(rho^2) > tau exactly: it is evaluated whenever rho^2 lies
+// within a relative 1e-12 of tau^2, where rho^2 > tau^2 could disagree.
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
 
@@ -23,7 +33,7 @@ namespace {
 
 struct Args64 {
     int64_t n;
-    double wave, tau, sg;
+    double wave, tau, tau2, sg;
     const double4_32a *pos, *nrm;
     const double4_32a *dens;  // (w_s p_re, w_s p_im, pt_re, pt_im)
     const double *p_re, *p_im, *pt_re, *pt_im;
@@ -50,6 +60,28 @@ __global__ void prep64_kernel(int64_t n, const double4_32a *__restrict__ nrm, co
     }
 }
 
+constexpr int kSinTable = 128;
+
+// sin and cos of x >= 0 by table lookup + short series (see the header).
+__device__ __forceinline__ void table_sincos(double x, const double2 *tab, double &s, double &c)
+{
+    // 2 pi / 128 split so that m * kStepHi is exact for m < 2^22
+    const double kInvStep = 20.371832715762604;      // 128 / (2 pi)
+    const double kStepHi = 0.049087385210441425;     // 2 pi / 128 rounded to 31 significant bits
+    const double kStepLo = 1.899093908283185e-12;    // 2 pi / 128 - kStepHi
+    const double m = rint(x * kInvStep);
+    double r = fma(-m, kStepHi, x);
+    r = fma(-m, kStepLo, r);
+    const double2 t = tab[((int)m) & (kSinTable - 1)];
+    const double z = r * r;
+    // sin r = r - r^3/3! + r^5/5! - r^7/7!,  cos r = 1 - r^2/2! + r^4/4! - r^6/6!
+    const double ps = fma(fma(z, -1.0 / 5040.0, 1.0 / 120.0), z, -1.0 / 6.0);
+    const double sr = fma(r * z, ps, r);
+    const double cr = fma(fma(fma(z, -1.0 / 720.0, 1.0 / 24.0), z, -0.5), z, 1.0);
+    s = fma(t.x, cr, t.y * sr);
+    c = fma(t.y, cr, -(t.x * sr));
+}
+
 template <int MODE, bool DIR>
 __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
 {
@@ -58,6 +90,12 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
     __shared__ alignas(128) double4_32a sn[2][T];
     __shared__ alignas(128) double4_32a sd[2][T];
     __shared__ alignas(8) uint64_t bar[2];
+    __shared__ double2 tab[kSinTable];
+    for (int i = threadIdx.x; i < kSinTable; i += blockDim.x) {
+        double si, co;
+        sincospi((double)i / (kSinTable / 2), &si, &co);
+        tab[i] = make_double2(si, co);
+    }
     const double c4 = 1. / (4. * 3.14159265358979323846264338328);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < a.n;
@@ -104,12 +142,15 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
                 const double4_32a sn_ = sn[buf][j];
                 const double4_32a sd_ = sd[buf][j];
                 const double xmy1 = tp.x - sp_.x, xmy2 = tp.y - sp_.y, xmy3 = tp.z - sp_.z;
-                const double rho = sqrt(xmy1 * xmy1 + xmy2 * xmy2 + xmy3 * xmy3);
+                const double r2 = xmy1 * xmy1 + xmy2 * xmy2 + xmy3 * xmy3;
+                bool far = r2 > a.tau2;
+                if (fabs(r2 - a.tau2) <= 1e-12 * a.tau2) far = sqrt(r2) > a.tau;
                 double vAr = 0.0, vAi = 0.0, vHr = 0.0, vHi = 0.0;
-                if (rho > a.tau) {
-                    const double rec = 1. / rho;
+                if (far) {
+                    const double rec = rsqrt(r2);
+                    const double rho = r2 * rec;
                     double S, C;
-                    sincos(a.wave * rho, &S, &C);
+                    table_sincos(a.wave * rho, tab, S, C);
                     const double eS = S * rec, eC = C * rec;
                     const double denom = c4 * rec * rec;
                     const double ct1 = -1. * (a.wave * S + eC) * denom;
@@ -192,6 +233,7 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     a.n = c.n;
     a.wave = c.wave;
     a.tau = c.tau;
+    a.tau2 = c.tau * c.tau;
     a.sg = (c.interior == 1) ? -1.0 : 1.0;
     a.pos = r.pos;
     a.nrm = r.nrm;

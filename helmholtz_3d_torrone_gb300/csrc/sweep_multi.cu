@@ -1,0 +1,442 @@
+// sweep_multi.cu -- multi-right-hand-side pair sweeps: Q = A P for a block of
+// RB density vectors with one kernel evaluation per point pair.
+//
+// Every pair's kernel value (distance, phase, sin/cos, projection) is
+// computed once and multiplied into RB densities, so the per-RHS cost falls
+// from a full pair evaluation to four fused multiply-adds.  Both precisions
+// follow the single-vector sweeps (sweep_f32.cu, sweep_f64.cu) for the
+// kernel arithmetic, tiling, TMA staging and the near-field rules; the
+// densities of a tile are staged as RB/2 rows of two complex values each.
+#include "hz_internal.cuh"
+#include "bulk_copy.cuh"
+#include "krylov_multi.cuh"
+
+namespace hz {
+namespace {
+
+constexpr double kPi = 3.14159265358979323846264338328;
+constexpr int kRB = 8;  // right-hand sides per kernel pass
+
+// ------------------------------------------------------------------ FP32
+struct ArgsM32 {
+    int64_t n, npad;
+    int nr;  // right-hand sides in this pass (<= kRB)
+    float wave, kh, kl, tau2, guard_lo, guard_hi;
+    double tau, tau_far;
+    const float4 *pos, *nrm;
+    const float4 *dens;  // [kRB/2][npad]: (p'_{2q} re, im, p'_{2q+1} re, im)
+    const double4_32a *origin, *tpos, *pos64;
+    const int *perm;
+    const double *p_re, *p_im;  // [nr][n] (diagonal term)
+    double *q_re, *q_im;        // [nr][n]
+    unsigned *err;
+};
+
+__global__ void prepm32_kernel(int64_t n, int64_t npad, int nr, const int *__restrict__ perm,
+                               const double4_32a *__restrict__ tpos, const double *__restrict__ p_re,
+                               const double *__restrict__ p_im, double scale, float4 *__restrict__ dens)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < npad; s += (int64_t)gridDim.x * blockDim.x) {
+        const int c = perm[s];
+        const double ws = (c >= 0) ? tpos[s].w * scale : 0.0;
+#pragma unroll
+        for (int q = 0; q < kRB / 2; q++) {
+            float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+            if (c >= 0) {
+                const int r0 = 2 * q, r1 = 2 * q + 1;
+                if (r0 < nr) {
+                    v.x = (float)(ws * p_re[(int64_t)r0 * n + c]);
+                    v.y = (float)(ws * p_im[(int64_t)r0 * n + c]);
+                }
+                if (r1 < nr) {
+                    v.z = (float)(ws * p_re[(int64_t)r1 * n + c]);
+                    v.w = (float)(ws * p_im[(int64_t)r1 * n + c]);
+                }
+            }
+            dens[(int64_t)q * npad + s] = v;
+        }
+    }
+}
+
+template <bool DIR, bool NEAR>
+__device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, const float4 s_n, const float3 rel,
+                                        const float3 tn, float treg, const double4_32a &tp, int64_t src_slot,
+                                        const float4 *sd, int j, float (&acc)[2 * kRB])
+{
+    const float dx = rel.x - s_p.x, dy = rel.y - s_p.y, dz = rel.z - s_p.z;
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    bool near = false;
+    if (NEAR) {
+        near = r2 <= a.tau2;
+        if (r2 > a.guard_lo && r2 < a.guard_hi) {
+            const int c = a.perm[src_slot];
+            if (c >= 0) {
+                const double4_32a q = a.pos64[c];
+                const double x1 = tp.x - q.x, x2 = tp.y - q.y, x3 = tp.z - q.z;
+                const double rr2 = x1 * x1 + x2 * x2 + x3 * x3;
+                near = !(sqrt(rr2) > a.tau);
+            }
+        }
+    }
+    const float rinv = rsqrtf(r2);
+    const float rho = r2 * rinv;
+    const float nn = rintf(rho * a.kh);
+    float f = fmaf(rho, a.kh, -nn);
+    f = fmaf(rho, a.kl, f);
+    float S, C;
+    __sincosf(f * 6.28318530717958647692f, &S, &C);
+    const float u1 = fmaf(C, rinv, a.wave * S);
+    const float u2 = fmaf(a.wave, C, -S * rinv);
+    const float rr = rinv * rinv;
+    const float pA = DIR ? (dx * s_n.x + dy * s_n.y + dz * s_n.z) : (dx * tn.x + dy * tn.y + dz * tn.z);
+    float vr = -u1 * rr * pA, vi = u2 * rr * pA;
+    if (NEAR && near) {
+        vr = DIR ? s_p.w : treg;
+        vi = 0.f;
+    }
+#pragma unroll
+    for (int q = 0; q < kRB / 2; q++) {
+        const float4 d = sd[q * kTile32 + j];
+        acc[4 * q + 0] = fmaf(vr, d.x, fmaf(-vi, d.y, acc[4 * q + 0]));
+        acc[4 * q + 1] = fmaf(vr, d.y, fmaf(vi, d.x, acc[4 * q + 1]));
+        acc[4 * q + 2] = fmaf(vr, d.z, fmaf(-vi, d.w, acc[4 * q + 2]));
+        acc[4 * q + 3] = fmaf(vr, d.w, fmaf(vi, d.z, acc[4 * q + 3]));
+    }
+}
+
+constexpr int kNT32m = 256;
+constexpr size_t kSmemM32 = 2 * (2 + kRB / 2) * kTile32 * sizeof(float4);
+
+template <bool DIR>
+__global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
+{
+    constexpr int TS = kTile32;
+    extern __shared__ __align__(128) float4 smem32[];
+    __shared__ alignas(8) uint64_t bar[2];
+    float4 *sp[2] = {smem32, smem32 + (2 + kRB / 2) * TS};
+    const int64_t slot = (int64_t)blockIdx.x * kNT32m + threadIdx.x;
+    const double4_32a tp = a.tpos[slot];
+    const float4 nn4 = a.nrm[slot];
+    const float3 tn = make_float3(nn4.x, nn4.y, nn4.z);
+    const float treg = a.pos[slot].w;
+    const double4_32a tsph = a.origin[slot / TS];
+    double accd[2 * kRB];
+#pragma unroll
+    for (int i = 0; i < 2 * kRB; i++) accd[i] = 0.0;
+    const int64_t ntiles = a.npad / TS;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue = [&](int64_t tile, int buf) {
+        const int64_t base = tile * TS;
+        const uint32_t bytes = TS * sizeof(float4);
+        mbar_arrive_expect_tx(&bar[buf], (2 + kRB / 2) * bytes);
+        bulk_g2s(sp[buf], a.pos + base, bytes, &bar[buf]);
+        bulk_g2s(sp[buf] + TS, a.nrm + base, bytes, &bar[buf]);
+#pragma unroll
+        for (int q = 0; q < kRB / 2; q++) bulk_g2s(sp[buf] + (2 + q) * TS, a.dens + q * a.npad + base, bytes, &bar[buf]);
+    };
+    if (threadIdx.x == 0) issue(0, 0);
+    for (int64_t tile = 0; tile < ntiles; tile++) {
+        const int buf = (int)(tile & 1);
+        if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
+        const double4_32a o = a.origin[tile];
+        const double ex = o.x - tsph.x, ey = o.y - tsph.y, ez = o.z - tsph.z;
+        const bool far = sqrt(ex * ex + ey * ey + ez * ez) - o.w - tsph.w > a.tau_far;
+        const float3 rel = make_float3((float)(tp.x - o.x), (float)(tp.y - o.y), (float)(tp.z - o.z));
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, DEV_ERR_WAIT);
+                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
+            }
+            return;
+        }
+        const float4 *P = sp[buf], *Nn = sp[buf] + TS, *D = sp[buf] + 2 * TS;
+        float acc[2 * kRB];
+#pragma unroll
+        for (int i = 0; i < 2 * kRB; i++) acc[i] = 0.f;
+        const int64_t base = tile * TS;
+        if (far) {
+            for (int j = 0; j < TS; j++) pairm32<DIR, false>(a, P[j], Nn[j], rel, tn, treg, tp, base + j, D, j, acc);
+        } else {
+            for (int j = 0; j < TS; j++) pairm32<DIR, true>(a, P[j], Nn[j], rel, tn, treg, tp, base + j, D, j, acc);
+        }
+#pragma unroll
+        for (int i = 0; i < 2 * kRB; i++) accd[i] += acc[i];
+        __syncthreads();
+    }
+    const int c = a.perm[slot];
+    if (c < 0) return;
+#pragma unroll
+    for (int r = 0; r < kRB; r++) {
+        if (r >= a.nr) break;
+        const double vr = accd[2 * r], vi = accd[2 * r + 1];
+        if (!isfinite(vr) || !isfinite(vi)) atomicOr(a.err, DEV_ERR_NONFINITE);
+        a.q_re[(int64_t)r * a.n + c] = vr + 0.5 * a.p_re[(int64_t)r * a.n + c];
+        a.q_im[(int64_t)r * a.n + c] = vi + 0.5 * a.p_im[(int64_t)r * a.n + c];
+    }
+}
+
+// ------------------------------------------------------------------ FP64
+constexpr int kSinTable = 128;
+constexpr int kT64m = 128;  // sources per tile = threads per block
+
+__device__ __forceinline__ void table_sincos_m(double x, const double2 *tab, double &s, double &c)
+{
+    // the same table-driven method as sweep_f64.cu
+    const double kInvStep = 20.371832715762604;
+    const double kStepHi = 0.049087385210441425;
+    const double kStepLo = 1.899093908283185e-12;
+    const double m = rint(x * kInvStep);
+    double r = fma(-m, kStepHi, x);
+    r = fma(-m, kStepLo, r);
+    const double2 t = tab[((int)m) & (kSinTable - 1)];
+    const double z = r * r;
+    const double ps = fma(fma(z, -1.0 / 5040.0, 1.0 / 120.0), z, -1.0 / 6.0);
+    const double sr = fma(r * z, ps, r);
+    const double cr = fma(fma(fma(z, -1.0 / 720.0, 1.0 / 24.0), z, -0.5), z, 1.0);
+    s = fma(t.x, cr, t.y * sr);
+    c = fma(t.y, cr, -(t.x * sr));
+}
+
+struct ArgsM64 {
+    int64_t n;
+    int nr;
+    double wave, tau, tau2, sg;
+    const double4_32a *pos, *nrm;
+    const double4_32a *dens;  // [kRB/2][n]: (w p_{2q}, w p_{2q+1})
+    const double *p_re, *p_im;
+    double *q_re, *q_im;
+    unsigned *err;
+};
+
+__global__ void prepm64_kernel(int64_t n, int nr, const double4_32a *__restrict__ nrm, const double *__restrict__ p_re,
+                               const double *__restrict__ p_im, double4_32a *__restrict__ dens)
+{
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+        const double w = nrm[s].w;
+#pragma unroll
+        for (int q = 0; q < kRB / 2; q++) {
+            const int r0 = 2 * q, r1 = 2 * q + 1;
+            double4_32a v = make_double4_32a(0, 0, 0, 0);
+            if (r0 < nr) {
+                v.x = w * p_re[(int64_t)r0 * n + s];
+                v.y = w * p_im[(int64_t)r0 * n + s];
+            }
+            if (r1 < nr) {
+                v.z = w * p_re[(int64_t)r1 * n + s];
+                v.w = w * p_im[(int64_t)r1 * n + s];
+            }
+            dens[(int64_t)q * n + s] = v;
+        }
+    }
+}
+
+constexpr size_t kSmemM64 = 2 * (2 + kRB / 2) * kT64m * sizeof(double4_32a);
+
+template <bool DIR>
+__global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
+{
+    constexpr int T = kT64m;
+    extern __shared__ __align__(128) double4_32a smem64[];
+    __shared__ alignas(8) uint64_t bar[2];
+    __shared__ double2 tab[kSinTable];
+    for (int i = threadIdx.x; i < kSinTable; i += blockDim.x) {
+        double si, co;
+        sincospi((double)i / (kSinTable / 2), &si, &co);
+        tab[i] = make_double2(si, co);
+    }
+    double4_32a *sp[2] = {smem64, smem64 + (2 + kRB / 2) * T};
+    const double c4 = 1. / (4. * kPi);
+    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    const bool valid = t < a.n;
+    double4_32a tp = make_double4_32a(0, 0, 0, 0), tn = make_double4_32a(0, 0, 0, 0);
+    if (valid) {
+        tp = a.pos[t];
+        tn = a.nrm[t];
+    }
+    double acc[2 * kRB];
+#pragma unroll
+    for (int i = 0; i < 2 * kRB; i++) acc[i] = 0.0;
+    const int64_t ntiles = (a.n + T - 1) / T;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    auto issue = [&](int64_t tile, int buf) {
+        const int64_t base = tile * T;
+        const int64_t cnt = (a.n - base < T) ? (a.n - base) : T;
+        const uint32_t bytes = (uint32_t)(cnt * sizeof(double4_32a));
+        mbar_arrive_expect_tx(&bar[buf], (2 + kRB / 2) * bytes);
+        bulk_g2s(sp[buf], a.pos + base, bytes, &bar[buf]);
+        bulk_g2s(sp[buf] + T, a.nrm + base, bytes, &bar[buf]);
+#pragma unroll
+        for (int q = 0; q < kRB / 2; q++) bulk_g2s(sp[buf] + (2 + q) * T, a.dens + q * a.n + base, bytes, &bar[buf]);
+    };
+    if (threadIdx.x == 0 && ntiles > 0) issue(0, 0);
+    for (int64_t tile = 0; tile < ntiles; tile++) {
+        const int buf = (int)(tile & 1);
+        if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, DEV_ERR_WAIT);
+                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
+            }
+            return;
+        }
+        const int64_t base = tile * T;
+        const int cnt = (int)((a.n - base < T) ? (a.n - base) : T);
+        const double4_32a *P = sp[buf], *Nn = sp[buf] + T, *D = sp[buf] + 2 * T;
+        if (valid) {
+            for (int j = 0; j < cnt; j++) {
+                const double4_32a s_p = P[j], s_n = Nn[j];
+                const double xmy1 = tp.x - s_p.x, xmy2 = tp.y - s_p.y, xmy3 = tp.z - s_p.z;
+                const double r2 = xmy1 * xmy1 + xmy2 * xmy2 + xmy3 * xmy3;
+                bool far = r2 > a.tau2;
+                if (fabs(r2 - a.tau2) <= 1e-12 * a.tau2) far = sqrt(r2) > a.tau;
+                double vr, vi;
+                if (far) {
+                    const double rec = rsqrt(r2);
+                    const double rho = r2 * rec;
+                    double S, C;
+                    table_sincos_m(a.wave * rho, tab, S, C);
+                    const double denom = c4 * rec * rec;
+                    const double ct1 = -1. * (a.wave * S + C * rec) * denom;
+                    const double ct2 = (a.wave * C - S * rec) * denom;
+                    const double in = DIR ? (xmy1 * s_n.x + xmy2 * s_n.y + xmy3 * s_n.z)
+                                          : (xmy1 * tn.x + xmy2 * tn.y + xmy3 * tn.z);
+                    vr = a.sg * ct1 * in;
+                    vi = a.sg * ct2 * in;
+                } else {
+                    vr = DIR ? s_p.w : tp.w;
+                    vi = 0.0;
+                }
+#pragma unroll
+                for (int q = 0; q < kRB / 2; q++) {
+                    const double4_32a d = D[q * T + j];
+                    acc[4 * q + 0] += vr * d.x - vi * d.y;
+                    acc[4 * q + 1] += vr * d.y + vi * d.x;
+                    acc[4 * q + 2] += vr * d.z - vi * d.w;
+                    acc[4 * q + 3] += vr * d.w + vi * d.z;
+                }
+            }
+        }
+        __syncthreads();
+    }
+    if (!valid) return;
+#pragma unroll
+    for (int r = 0; r < kRB; r++) {
+        if (r >= a.nr) break;
+        const double vr = acc[2 * r], vi = acc[2 * r + 1];
+        if (!isfinite(vr) || !isfinite(vi)) atomicOr(a.err, DEV_ERR_NONFINITE);
+        a.q_re[(int64_t)r * a.n + t] = vr + 0.5 * a.p_re[(int64_t)r * a.n + t];
+        a.q_im[(int64_t)r * a.n + t] = vi + 0.5 * a.p_im[(int64_t)r * a.n + t];
+    }
+}
+
+int blocks_for(int64_t work)
+{
+    long long b = (work + 255) / 256;
+    if (b > 4096) b = 4096;
+    return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+void split_wave(double wave, float &kh, float &kl);  // sweep_f32.cu
+
+int multi_rhs_block() { return kRB; }
+
+size_t multi_rhs_scratch_bytes(int64_t n, int64_t npad)
+{
+    const size_t a = (size_t)(kRB / 2) * (size_t)npad * sizeof(float4);
+    const size_t b = (size_t)(kRB / 2) * (size_t)n * sizeof(double4_32a);
+    return a > b ? a : b;
+}
+
+int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int precision, int nrhs,
+                const double *p_re, const double *p_im, double *q_re, double *q_im, void *scratch,
+                cudaStream_t s)
+{
+    if (c.n <= 0 || nrhs <= 0) return HZ_OK;
+    for (int r0 = 0; r0 < nrhs; r0 += kRB) {
+        const int nr = (nrhs - r0 < kRB) ? (nrhs - r0) : kRB;
+        const double *pr = p_re + (int64_t)r0 * c.n, *pi = p_im + (int64_t)r0 * c.n;
+        double *qr = q_re + (int64_t)r0 * c.n, *qi = q_im + (int64_t)r0 * c.n;
+        if (precision == HZ_PREC_F64) {
+            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmemM64));
+            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmemM64));
+            double4_32a *dens = static_cast<double4_32a *>(scratch);
+            prepm64_kernel<<<blocks_for(c.n), 256, 0, s>>>(c.n, nr, r64.nrm, pr, pi, dens);
+            HZ_CHECK_LAUNCH();
+            ArgsM64 a;
+            a.n = c.n;
+            a.nr = nr;
+            a.wave = c.wave;
+            a.tau = c.tau;
+            a.tau2 = c.tau * c.tau;
+            a.sg = (c.interior == 1) ? -1.0 : 1.0;
+            a.pos = r64.pos;
+            a.nrm = r64.nrm;
+            a.dens = dens;
+            a.p_re = pr;
+            a.p_im = pi;
+            a.q_re = qr;
+            a.q_im = qi;
+            a.err = c.err;
+            const unsigned blocks = (unsigned)((c.n + kT64m - 1) / kT64m);
+            if (c.dirichlet) sweepm64_kernel<true><<<blocks, kT64m, kSmemM64, s>>>(a);
+            else sweepm64_kernel<false><<<blocks, kT64m, kSmemM64, s>>>(a);
+            HZ_CHECK_LAUNCH();
+        } else {
+            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmemM32));
+            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                               (int)kSmemM32));
+            float4 *dens = static_cast<float4 *>(scratch);
+            const double scale = ((c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi);
+            prepm32_kernel<<<blocks_for(r32.npad), 256, 0, s>>>(c.n, r32.npad, nr, r32.perm, r32.tpos, pr, pi, scale,
+                                                                dens);
+            HZ_CHECK_LAUNCH();
+            ArgsM32 a;
+            a.n = c.n;
+            a.npad = r32.npad;
+            a.nr = nr;
+            a.wave = (float)c.wave;
+            split_wave(c.wave, a.kh, a.kl);
+            a.tau = c.tau;
+            a.tau_far = c.tau * (1.0 + 1e-3);
+            a.tau2 = (float)(c.tau * c.tau);
+            a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
+            a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
+            a.pos = r32.pos;
+            a.nrm = r32.nrm;
+            a.dens = dens;
+            a.origin = r32.origin;
+            a.tpos = r32.tpos;
+            a.pos64 = r64.pos;
+            a.perm = r32.perm;
+            a.p_re = pr;
+            a.p_im = pi;
+            a.q_re = qr;
+            a.q_im = qi;
+            a.err = c.err;
+            const unsigned blocks = (unsigned)(r32.npad / kNT32m);
+            if (c.dirichlet) sweepm32_kernel<true><<<blocks, kNT32m, kSmemM32, s>>>(a);
+            else sweepm32_kernel<false><<<blocks, kNT32m, kSmemM32, s>>>(a);
+            HZ_CHECK_LAUNCH();
+        }
+    }
+    return HZ_OK;
+}
+
+}  // namespace hz

@@ -187,6 +187,7 @@ struct InitArgs {
     int64_t n;
     const int64_t *idx;
     double *xs, *nrm, *delta, *jac, *reg, *w;
+    double *dreg;  // d reg / d k (for wave-number gradients), may be NULL
     double4_32a *pos64, *nrm64;
     unsigned *err;
 };
@@ -277,6 +278,11 @@ __global__ void __launch_bounds__(256) init_kernel(InitArgs a)
         const double r3 = -25. * tau * (2. * cm) * cg / (1536. * PI);
         const double r4 = a.wave * a.wave * tau * 2. * cm / (48. * PI);
         const double reg = (a.interior == 1) ? (r1 + r2 + r3 + r4) : -1. * (r1 + r2 + r3 + r4);
+        // only r4 = k^2 tau 2H / (48 pi) depends on k
+        if (a.dreg) {
+            const double d4 = 2.0 * a.wave * tau * 2. * cm / (48. * PI);
+            a.dreg[c] = (a.interior == 1) ? d4 : -d4;
+        }
         const double w = a.HC * delta * jac;  // :4447
         if (!isfinite(w) || !isfinite(reg)) bad |= DEV_ERR_NONFINITE;
         a.xs[3 * c] = tx;
@@ -317,7 +323,8 @@ __global__ void __launch_bounds__(kTile32) rec32_kernel(const int *__restrict__ 
                                                         const double4_32a *__restrict__ pos64,
                                                         const double4_32a *__restrict__ nrm64,
                                                         float4 *__restrict__ pos32, float4 *__restrict__ nrm32,
-                                                        double4_32a *__restrict__ origin, double4_32a *__restrict__ tpos)
+                                                        double4_32a *__restrict__ origin, double4_32a *__restrict__ tpos,
+                                                        double reg_scale)
 {
     const int64_t s = (int64_t)blockIdx.x * kTile32 + threadIdx.x;
     const int c = perm[s];
@@ -342,7 +349,7 @@ __global__ void __launch_bounds__(kTile32) rec32_kernel(const int *__restrict__ 
         }
     }
     __syncthreads();
-    __shared__ double org[3];
+    __shared__ double org[3], ext[3];
     if (threadIdx.x < 3) {
         double a0 = 1e300, a1 = -1e300;
         for (int w = 0; w < kTile32 / 32; w++) {
@@ -350,11 +357,17 @@ __global__ void __launch_bounds__(kTile32) rec32_kernel(const int *__restrict__ 
             a1 = fmax(a1, hi[threadIdx.x][w]);
         }
         org[threadIdx.x] = (a0 <= a1) ? 0.5 * (a0 + a1) : 0.0;
+        ext[threadIdx.x] = (a0 <= a1) ? 0.5 * (a1 - a0) : 0.0;
     }
     __syncthreads();
-    if (threadIdx.x == 0) origin[blockIdx.x] = make_double4_32a(org[0], org[1], org[2], 0.0);
+    // .w = radius of a sphere around the origin that holds every point of
+    // the tile (half the bounding-box diagonal, rounded up a little)
+    if (threadIdx.x == 0)
+        origin[blockIdx.x] = make_double4_32a(org[0], org[1], org[2],
+                                              sqrt(ext[0] * ext[0] + ext[1] * ext[1] + ext[2] * ext[2]) * (1.0 + 1e-12));
     if (c >= 0) {
-        pos32[s] = make_float4((float)(p.x - org[0]), (float)(p.y - org[1]), (float)(p.z - org[2]), (float)p.w);
+        pos32[s] = make_float4((float)(p.x - org[0]), (float)(p.y - org[1]), (float)(p.z - org[2]),
+                               (float)(p.w * reg_scale));
         nrm32[s] = make_float4((float)q.x, (float)q.y, (float)q.z, (float)q.w);
         tpos[s] = make_double4_32a(p.x, p.y, p.z, q.w);
     } else {
@@ -387,9 +400,10 @@ int tube_build(int N, double eps, const double *d, DevBuf &idx, int64_t &n, DevB
 int tube_init(const hz_params &p, const double *d, const double *gx, const double *gy, const double *gz,
               const double *mc, const double *gc, int64_t n, const int64_t *idx, double *xs, double *nrm,
               double *delta, double *jac, double *reg, double *w, double4_32a *pos64, double4_32a *nrm64,
-              unsigned *err, cudaStream_t s)
+              unsigned *err, cudaStream_t s, double *dreg)
 {
     InitArgs a;
+    a.dreg = dreg;
     a.N = p.N;
     a.H = (p.int_u - p.int_l) / p.N;
     a.int_l = p.int_l;
@@ -436,10 +450,12 @@ int sweep_order(int N, int64_t n, const int64_t *idx, int *perm, int64_t npad, D
 }
 
 int build_rec32(int64_t n, int64_t npad, const int *perm, const double4_32a *pos64, const double4_32a *nrm64,
-                float4 *pos32, float4 *nrm32, double4_32a *origin, double4_32a *tpos, cudaStream_t s)
+                float4 *pos32, float4 *nrm32, double4_32a *origin, double4_32a *tpos, double reg_scale,
+                cudaStream_t s)
 {
     (void)n;
-    rec32_kernel<<<(unsigned)(npad / kTile32), kTile32, 0, s>>>(perm, pos64, nrm64, pos32, nrm32, origin, tpos);
+    rec32_kernel<<<(unsigned)(npad / kTile32), kTile32, 0, s>>>(perm, pos64, nrm64, pos32, nrm32, origin, tpos,
+                                                                 reg_scale);
     HZ_CHECK_LAUNCH();
     return HZ_OK;
 }

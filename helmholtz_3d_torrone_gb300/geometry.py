@@ -53,8 +53,22 @@ def ellipsoid(N, axes=(0.7, 0.5, 0.4), int_l=-1.0, int_u=1.0, iters=60):
         r = a[None, :] * y / den
         F = np.sum(r * r, axis=1) - 1.0
         dF = -2.0 * np.sum(r * r / den, axis=1)
-        t = np.maximum(t - F / dF, floor)
+        step = np.divide(F, dF, out=np.zeros_like(F), where=dF != 0)
+        t = np.maximum(t - step, floor)
     x = a[None, :] ** 2 * y / (t[:, None] + a[None, :] ** 2)
+    # Degenerate case (point on the plane of the shortest axis, inside the
+    # evolute): the root sits at t = -min a_i^2 and the closest point leaves
+    # that plane; solve for its shortest-axis coordinate from the surface.
+    im = int(np.argmin(a))
+    deg = t <= floor * (1.0 - 1e-9)
+    if np.any(deg):
+        others = [i for i in range(3) if i != im]
+        xd = np.zeros((int(deg.sum()), 3))
+        for i in others:
+            xd[:, i] = a[i] ** 2 * y[deg, i] / (a[i] ** 2 - a[im] ** 2)
+        rest = 1.0 - sum((xd[:, i] / a[i]) ** 2 for i in others)
+        xd[:, im] = a[im] * np.sqrt(np.maximum(rest, 0.0))
+        x[deg] = xd
     dist = np.sqrt(np.sum((x - y) ** 2, axis=1))
     s = np.where(inside, dist, -dist)
     return np.ascontiguousarray(s.reshape(shape))
@@ -76,3 +90,26 @@ def random_sphere_points(m, radius, seed):
     v = rng.normal(size=(m, 3))
     v /= np.linalg.norm(v, axis=1, keepdims=True)
     return radius * v
+
+
+def ellipsoid_levelset(N, axes=(0.7, 0.5, 0.4), scale=0.3, int_l=-1.0, int_u=1.0):
+    """A smooth level set of an ellipsoid that is not a distance function
+    (positive inside): scale * (1 - sqrt(sum x_i^2 / a_i^2)).  Feed it to the
+    reinitialisation to obtain the signed distance."""
+    H, X, Y, Z = node_coords(N, int_l, int_u)
+    a = np.asarray(axes, dtype=np.float64)
+    phi = scale * (1.0 - np.sqrt(X ** 2 / a[0] ** 2 + Y ** 2 / a[1] ** 2 + Z ** 2 / a[2] ** 2))
+    return np.ascontiguousarray(np.broadcast_to(phi, (N + 1,) * 3))
+
+
+def bumpy_sphere_levelset(N, r0=0.5, amp=0.08, int_l=-1.0, int_u=1.0):
+    """Level set r(theta, phi) - |x| of the bumpy sphere
+    r(theta, phi) = r0 (1 + amp cos(3 theta) sin(2 phi)) (positive inside,
+    theta polar from +z, phi azimuth); not a distance function."""
+    H, X, Y, Z = node_coords(N, int_l, int_u)
+    shape = (N + 1,) * 3
+    X, Y, Z = (np.broadcast_to(a, shape) for a in (X, Y, Z))
+    rad = np.sqrt(X ** 2 + Y ** 2 + Z ** 2)
+    theta = np.arccos(np.clip(np.divide(Z, rad, out=np.zeros(shape), where=rad > 0), -1.0, 1.0))
+    ph = np.arctan2(Y, X)
+    return np.ascontiguousarray(r0 * (1.0 + amp * np.cos(3 * theta) * np.sin(2 * ph)) - rad)

@@ -62,6 +62,8 @@ extern "C" {
 #define HZ_BICG 0     /* complex BiCG with A and A^H: BICGSTAB.c:5-339 (CompBiCG)  */
 #define HZ_BICGSTAB 1 /* complex BiCGSTAB (the reference's real BiCGSTAB,
                          large3Dexample2.c:2265-2477, in complex arithmetic)      */
+#define HZ_GMRES 2    /* restarted GMRES(restart), FP64 vectors, classical Gram-
+                         Schmidt applied twice; A products only (no A^H)        */
 
 /* Evaluation layers. */
 #define HZ_SINGLE_LAYER 0 /* NeumannTest, large3Dexample2.c:1810-1824 */
@@ -91,13 +93,16 @@ typedef struct hz_params {
 typedef struct hz_operator hz_operator;
 
 typedef struct hz_solve_opts {
-    int method;        /* HZ_BICG or HZ_BICGSTAB                                        */
+    int method;        /* HZ_BICG, HZ_BICGSTAB or HZ_GMRES                              */
     int precision;     /* HZ_PREC_*                                                     */
     double tol;        /* stop at ||b - A x|| / ||b|| < tol (reference DEFAULTACC 1e-7) */
     int maxit;         /* Krylov iteration cap (reference: 2000)                        */
-    double inner_tol;  /* HZ_PREC_F32_REFINED: relative tolerance of each inner solve   */
+    double inner_tol;  /* HZ_PREC_F32_REFINED: relative tolerance of each inner solve
+                          (FP32 densities bound it near 1e-7; an inner solve also
+                          stops after 30 iterations without a new minimum)       */
     int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap                      */
     int stagnation;    /* 1: also stop when |delta(||r||/||b||)| < 1e-3 tol (reference) */
+    int restart;       /* HZ_GMRES: Krylov basis size before a restart (2..127)         */
 } hz_solve_opts;
 
 typedef struct hz_solve_info {
@@ -134,6 +139,13 @@ HZ_API int hz_set_distance(hz_operator *op, const double *d, int where);
 HZ_API int hz_build(hz_operator *op, int64_t *n);
 HZ_API int64_t hz_tube_size(const hz_operator *op);
 
+/* Autotuner: times every compiled variant of the FP32 pair sweep (block
+ * shape x targets per thread) on this operator's tube and keeps the
+ * fastest for all later FP32 sweeps.  Returns the chosen variant and its
+ * time for one fused A p + A^H pt sweep.  hz_set_sweep_config forces one. */
+HZ_API int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep);
+HZ_API int hz_set_sweep_config(hz_operator *op, int cfg);
+
 /* Per-kernel timing of the pair sweeps: CUDA events recorded on the launch
  * stream around every sweep kernel (also inside the solver's iteration
  * graphs).  enable = 1 / 0 switches it on / off and clears the totals,
@@ -158,14 +170,43 @@ HZ_API int hz_matvec_pair(hz_operator *op, int precision, const double *p_re, co
                    const double *pt_re, const double *pt_im, double *q_re, double *q_im,
                    double *qt_re, double *qt_im, int where);
 /* Multi right-hand side: Q = A P for nrhs column vectors stored one after
- * the other (vector r at offset r*n), one kernel evaluation per pair. */
+ * the other (vector r at offset r*n), one kernel evaluation per pair and
+ * block of 8 right-hand sides. */
 HZ_API int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re,
                     const double *p_im, double *q_re, double *q_im, int where);
+
+/* Solve A X = B for nrhs right-hand sides ([nrhs][n] each) with BiCGSTAB in
+ * lockstep over the columns, every product a multi right-hand-side sweep;
+ * HZ_PREC_F32_REFINED refines every column with FP64 residuals.  resid (may
+ * be NULL) receives each column's final relative residual. */
+HZ_API int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts, int nrhs, const double *b_re,
+                          const double *b_im, double *x_re, double *x_im, int where,
+                          hz_solve_info *info, double *resid);
+
+/* Incident plane waves e^{ik d.x} for ndir unit directions (3 doubles each,
+ * host memory): kind HZ_RHS_POINT_DIRICHLET gives the values at the
+ * projected points, HZ_RHS_POINT_NEUMANN the outward normal derivative.
+ * Output [ndir][n]. */
+HZ_API int hz_rhs_plane_waves(hz_operator *op, int ndir, const double *dirs, int kind, double *b_re,
+                              double *b_im, int where);
 
 /* Solve A x = b (x0 = 0).  opts may be NULL: BiCG, FP64, tol 1e-7, 2000 its. */
 HZ_API int hz_solve(hz_operator *op, const hz_solve_opts *opts, const double *b_re, const double *b_im,
              double *x_re, double *x_im, int where, hz_solve_info *info);
 HZ_API void hz_solve_opts_default(hz_solve_opts *o);
+
+/* Receiver misfit and its gradients by the adjoint method.
+ * J = sum_m |u(x_m) - t_m|^2 with u = E sigma (layer as in hz_eval) and
+ * A sigma = b.  One forward solve, one adjoint solve A^H lambda = E^H r
+ * (r = u - t), and recomputed kernel derivatives give
+ *   g = dJ/d(Re b) + i dJ/d(Im b) = 2 lambda                    (n values),
+ *   dJ/dk at fixed b = 2 Re(r^H dE/dk sigma) - 2 Re(lambda^H dA/dk sigma),
+ *   dJ/dw_s = Re(conj(lambda_s) sigma_s) / w_s   (tube-point weights, n).
+ * Any output pointer may be NULL.  opts as for hz_solve (both solves). */
+HZ_API int hz_misfit_gradient(hz_operator *op, const hz_solve_opts *opts, const double *b_re,
+                              const double *b_im, int layer, int64_t m, const double *rx,
+                              const double *t_re, const double *t_im, double *J, double *g_re,
+                              double *g_im, double *dJ_dk, double *dJ_dw, int where, hz_solve_info *info);
 
 /* Boundary data at the projected points (see HZ_RHS_*). src: 3 doubles. */
 HZ_API int hz_rhs_point_source(hz_operator *op, const double *src, int kind, double *b_re, double *b_im,
@@ -183,6 +224,14 @@ HZ_API int hz_eval(hz_operator *op, int layer, int64_t m, const double *rx, cons
 HZ_API int hz_assign_gradient(int N, double H, const double *d, double *gx, double *gy, double *gz,
                        int weno_order, int where);
 HZ_API int hz_assign_curvatures(int N, double H, const double *d, double *mcurv, double *gcurv, int where);
+
+/* Reinitialise a level set toward the signed distance, in place: iters TVD
+ * Runge-Kutta-2 pseudo-time steps (dt = cfl*H, cfl <= 1) of
+ * phi_t + S(phi0)(|grad phi| - 1) = 0 with S(phi0) = phi0/sqrt(phi0^2+H^2),
+ * |grad phi| from the Godunov Hamiltonian of finite_difference3D.c:5-27 on
+ * WENO one-sided derivatives (weno.c:259-345, mirror boundaries).  The
+ * reference itself has no reinitialisation (its Godunov() is unused). */
+HZ_API int hz_reinitialize(int N, double H, double *phi, int iters, double cfl, int weno_order, int where);
 
 /* Dense complex BiCG on a caller-provided row-major n x n matrix (real and
  * imaginary parts): the device form of CompBiCG (BICGSTAB.c:5-339). */
@@ -216,6 +265,38 @@ HZ_API int hz_matvec_f64_noalloc(const hz_params *p, int64_t n, int adjoint, con
                                  const double *nrm, const double *reg, const double *w,
                                  const double *p_re, const double *p_im, double *q_re, double *q_im,
                                  void *stream);
+
+/* The reference driver's text files (host only, no device work):
+ * distance<N>.txt ((N+1)^3 values, (i,j,k) order, large3Dexample2.c:405-424),
+ * the boundary-data pair Rel_bN<N>k<k>.txt / Rel_bimgN<N>k<k>.txt (size line
+ * then "%.15lf" per line, :1236-1252,1333), the density pair
+ * Rel_DensityN<N>k<k>.txt / ...imgN... ("%.15lf " values, :3446-3474) and the
+ * NeumannTest log Rel_Result_N<N>k<k>.txt (:1885-1896).  Readers check the
+ * size line and report short or NaN data as errors. */
+HZ_API int hz_reference_file_names(int N, double wave, char *b, char *bimg, char *dens, char *densimg,
+                                   char *result, char *distance, size_t cap);
+HZ_API int hz_read_distance_file(const char *path, int N, double *d);
+HZ_API int hz_write_distance_file(const char *path, int N, const double *d);
+HZ_API int hz_write_rhs_files(const char *path_re, const char *path_im, int64_t n, const double *b_re,
+                              const double *b_im);
+HZ_API int hz_read_rhs_files(const char *path_re, const char *path_im, int64_t n, double *b_re,
+                             double *b_im);
+HZ_API int hz_write_density_files(const char *path_re, const char *path_im, int64_t n, const double *x_re,
+                                  const double *x_im);
+HZ_API int hz_read_density_files(const char *path_re, const char *path_im, int64_t n, double *x_re,
+                                 double *x_im);
+HZ_API int hz_write_result_file(const char *path, double exact_re, double exact_im, double approx_re,
+                                double approx_im);
+
+/* Field on a plane (the reference's slice printer, printslice.c:5-746, as a
+ * headless buffer): u at the n2 x n2 points lo + (a*h2, b*h2) of the plane
+ * axis = c (axis 0: x = c, points (c, y, z); 1: y = c, points (x, c, z);
+ * 2: z = c, points (x, y, c)), row a, column b, u[a*n2 + b].  Points whose
+ * interpolated distance exceeds -mask (inside the body or near it) are set
+ * to 0, as the reference prints 0 where distance() > -0.06. */
+HZ_API int hz_eval_slice(hz_operator *op, int layer, int axis, double c, int n2, double lo, double h2,
+                         double mask, const double *s_re, const double *s_im, double *u_re, double *u_im,
+                         int where);
 
 /* Measure the FP32 and FP64 FMA throughput of the current device (TFLOP/s,
  * one FMA = 2 FLOP), the roofline denominators of the pair sweeps. */

@@ -86,6 +86,7 @@ class Oracle:
         L.or_eval.argtypes = [P, C.c_int64, _dp, _dp, _dp, _dp, _dp, C.c_int64, _dp, _dp, _dp,
                               C.c_int, C.c_int]
         L.or_point_source_rhs.argtypes = [P, C.c_int64, _dp, _dp, _dp, C.c_int, _dp, _dp]
+        L.or_reinit.argtypes = [C.c_int, C.c_double, _dp, C.c_int, C.c_double, C.c_int]
 
     def weno(self, fi, dx, order=5):
         fi = np.ascontiguousarray(fi, dtype=np.float64)
@@ -98,6 +99,11 @@ class Oracle:
         g = [np.empty_like(d) for _ in range(3)]
         self.L.or_gradient(N, H, _d(d), _d(g[0]), _d(g[1]), _d(g[2]), order)
         return g
+
+    def reinit(self, N, H, phi, iters, cfl=0.5, order=5):
+        out = np.array(phi, dtype=np.float64, copy=True, order="C")
+        self.L.or_reinit(N, H, _d(out), iters, cfl, order)
+        return out
 
     def curvatures(self, N, H, d):
         d = np.ascontiguousarray(d, dtype=np.float64)
@@ -214,6 +220,7 @@ class Reference:
         L.ref_dense_rows.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int]
         L.ref_compbicg.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_rows_matvec.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
+        L.ref_double_layer.argtypes = [C.c_int, _dp, _dp, _dp]
         cfg = np.zeros(6)
         L.ref_config(_d(cfg))
         self.int_l, self.int_u, self.factor, self.tau_factor = cfg[:4]
@@ -267,6 +274,14 @@ class Reference:
         are, aim = np.empty((r1 - r0, n)), np.empty((r1 - r0, n))
         self.L.ref_dense_rows(n, r0, r1, _d(are), _d(aim), nthreads)
         return are, aim
+
+    def double_layer(self, n):
+        """DoubleLayerKernel: (per-point arrays dict, dense complex matrix)."""
+        pts = np.zeros((16, n))
+        are, aim = np.empty((n, n)), np.empty((n, n))
+        self.L.ref_double_layer(n, _d(pts), _d(are), _d(aim))
+        keys = ["zx", "zy", "zz", "xs", "ys", "zs", "dist", "gx", "gy", "gz", "delta", "jac", "reg", "regimg", "result"]
+        return {k: pts[i] for i, k in enumerate(keys)}, are + 1j * aim
 
     def rows_matvec(self, n, v, r0, r1, nthreads=os.cpu_count() or 1):
         vr = np.ascontiguousarray(v.real)

@@ -165,6 +165,59 @@ void or_gradient(int N, double H, const double *d, double *gx, double *gy, doubl
             }
 }
 
+/* finite_difference3D.c:5-27 (Godunov upwind |grad phi|). */
+static double godunov(double signage, double a, double b, double c, double d, double e, double f)
+{
+    double aplus = t_max(a, 0.0) * t_max(a, 0.0), aminus = t_min(a, 0.0) * t_min(a, 0.0);
+    double bplus = t_max(b, 0.0) * t_max(b, 0.0), bminus = t_min(b, 0.0) * t_min(b, 0.0);
+    double cplus = t_max(c, 0.0) * t_max(c, 0.0), cminus = t_min(c, 0.0) * t_min(c, 0.0);
+    double dplus = t_max(d, 0.0) * t_max(d, 0.0), dminus = t_min(d, 0.0) * t_min(d, 0.0);
+    double eplus = t_max(e, 0.0) * t_max(e, 0.0), eminus = t_min(e, 0.0) * t_min(e, 0.0);
+    double fplus = t_max(f, 0.0) * t_max(f, 0.0), fminus = t_min(f, 0.0) * t_min(f, 0.0);
+    if (signage > 0) return sqrt(t_max(aminus, bplus) + t_max(cminus, dplus) + t_max(eminus, fplus));
+    if (signage < 0) return sqrt(t_max(aplus, bminus) + t_max(cplus, dminus) + t_max(eplus, fminus));
+    return 0.0;
+}
+
+/* One stage of phi_t + S(phi0)(|grad phi| - 1) = 0 (see or_reinit). */
+static void reinit_stage(int N, double H, double dt, const double *phi0, const double *phi, const double *base,
+                         double w0, double w1, double *out, int order)
+{
+    const int S = N + 1;
+#pragma omp parallel for schedule(static)
+    for (int i = 0; i < S; i++)
+        for (int j = 0; j < S; j++)
+            for (int k = 0; k < S; k++) {
+                double Dxp, Dxn, Dyp, Dyn, Dzp, Dzn;
+                weno_axis(phi, N, H, i, j, k, 0, order, &Dxp, &Dxn);
+                weno_axis(phi, N, H, i, j, k, 1, order, &Dyp, &Dyn);
+                weno_axis(phi, N, H, i, j, k, 2, order, &Dzp, &Dzn);
+                size_t o = IDX(i, j, k);
+                double p0 = phi0[o];
+                double sgn = p0 / sqrt(p0 * p0 + H * H);
+                double g = godunov(p0, Dxp, Dxn, Dyp, Dyn, Dzp, Dzn);
+                double stage = phi[o] - dt * sgn * (g - 1.0);
+                out[o] = (w0 != 0.0) ? (w0 * base[o] + w1 * stage) : stage;
+            }
+}
+
+void or_reinit(int N, double H, double *phi, int iters, double cfl, int order)
+{
+    const size_t S = (size_t)N + 1, total = S * S * S;
+    double *phi0 = malloc(total * sizeof(double)), *t1 = malloc(total * sizeof(double));
+    double *t2 = malloc(total * sizeof(double));
+    memcpy(phi0, phi, total * sizeof(double));
+    const double dt = cfl * H;
+    for (int it = 0; it < iters; it++) {
+        reinit_stage(N, H, dt, phi0, phi, phi, 0.0, 1.0, t1, order);
+        reinit_stage(N, H, dt, phi0, t1, phi, 0.5, 0.5, t2, order);
+        memcpy(phi, t2, total * sizeof(double));
+    }
+    free(phi0);
+    free(t1);
+    free(t2);
+}
+
 /* ------------------------------------------------------------------ */
 /* Second differences (finite_difference3D.c:220-390)                  */
 /* ------------------------------------------------------------------ */

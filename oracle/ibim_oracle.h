@@ -58,6 +58,12 @@ double or_dyz(const double *d, int N, double H, int i, int j, int k);
 /* distance_application3D.c:35-53 over every node (loop large3Dexample2.c:446-455). */
 void or_curvatures(int N, double H, const double *d, double *mcurv, double *gcurv);
 
+/* Level-set reinitialisation (absent from the reference; scheme from its
+ * unused Godunov(), finite_difference3D.c:5-27): iters TVD-RK2 steps of
+ * phi_t + S(phi0)(|grad phi| - 1) = 0, S = phi0/sqrt(phi0^2+H^2), WENO
+ * one-sided derivatives, dt = cfl*H.  In place. */
+void or_reinit(int N, double H, double *phi, int iters, double cfl, int order);
+
 /* Tube {|d| <= eps} in lexicographic (i,j,k) order, large3Dexample2.c:548-597.
  * Writes linear node indices into idx (may be NULL); returns the count. */
 int64_t or_tube(int N, const double *d, double eps, int64_t *idx);

@@ -40,6 +40,11 @@ double cal_delta(double epsilon, double x);
 double omp_get_Ccomp(int size, int pi, int pj, double epsilon, double tempC[]);
 int CompBiCG(int size, double *density, double *densityimg, double **Kernel, double **Kernelimg,
              double *b, double *bimg);
+int DoubleLayerKernel(int size, double epsilon, double ***level, double ***leveldx, double ***leveldy,
+                      double ***leveldz, double ***levelmcurv, double ***levelgcurv, double *zxlist, double *zylist,
+                      double *zzlist, double *zxstarlist, double *zystarlist, double *zzstarlist, double *dist,
+                      double *gradx, double *grady, double *gradz, double *delta, double *Jacobian, double *regfactor,
+                      double *regfactorimg, double *result, double **Kernel, double **Kernelimg, double wavenum);
 
 static double ***alloc_grid(int S)
 {
@@ -225,6 +230,27 @@ void ref_rows_matvec(int n, int r0, int r1, const double *pre, const double *pim
         qre[i - r0] = sr;
         qim[i - r0] = si;
     }
+}
+
+/* DoubleLayerKernel (HelmholtzKernel.c:613-761): per-point arrays (16 x n,
+ * in the order zx zy zz x* y* z* dist gx gy gz delta J reg regimg result
+ * and an unused row) and the dense matrix, row-major. */
+int ref_double_layer(int n, double *pts, double *are, double *aim)
+{
+    double eps = FACTOR * H;
+    double *a[16];
+    for (int r = 0; r < 16; r++) a[r] = pts + (size_t)r * n;
+    double **K = (double **)malloc(n * sizeof(double *));
+    double **Ki = (double **)malloc(n * sizeof(double *));
+    for (int i = 0; i < n; i++) {
+        K[i] = are + (size_t)i * n;
+        Ki[i] = aim + (size_t)i * n;
+    }
+    int rc = DoubleLayerKernel(n, eps, DIST, DIST_DX, DIST_DY, DIST_DZ, MCURV, GCURV, a[0], a[1], a[2], a[3], a[4],
+                               a[5], a[6], a[7], a[8], a[9], a[10], a[11], a[12], a[13], a[14], K, Ki, WAVE);
+    free(K);
+    free(Ki);
+    return rc;
 }
 
 /* CompBiCG (BICGSTAB.c:5-339) on a row-major dense matrix. */

@@ -8,6 +8,7 @@ Tolerances:
   * delta_eps and w: 1e-15 relative (CUDA cos vs. the C library's);
   * FP64 matvec: 1e-12 relative (summation order differs);
   * FP64 BiCG density solved to 1e-13: 1e-10 relative (north-star bound);
+  * GMRES (FP64 or FP32 + FP64 refinement) to 1e-12 / 1e-11: 1e-9 relative;
   * FP32 sweep vs FP64: 2e-5 relative (FP32 arithmetic).
 """
 import json
@@ -112,6 +113,23 @@ def test_bicgstab_and_refined_agree(hz, built, case):
     assert rel_err(xr, g["x"]) < 1e-9
     xs, iS = op.solve(g["b"], method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=1e-11, inner_tol=1e-5)
     assert rel_err(xs, g["x"]) < 1e-9
+
+
+@pytest.mark.parametrize("case", CASES)
+def test_gmres_vs_reference(hz, built, case):
+    """Restarted GMRES (FP64, and as the inner solver of the refinement)
+    reaches the reference's CompBiCG density; its recurrence residual is the
+    true FP64 residual."""
+    op, g, m = built[case]
+    b = g["b"]
+    x, info = op.solve(b, method=hz.GMRES, precision=hz.PREC_F64, tol=1e-12, restart=20)
+    assert info["resid"] < 1e-12
+    true = np.linalg.norm(b - op.matvec(x)) / np.linalg.norm(b)
+    assert true < 5e-12
+    assert rel_err(x, g["x"]) < 1e-9
+    xr, ir = op.solve(b, method=hz.GMRES, precision=hz.PREC_F32_REFINED, tol=1e-11, inner_tol=1e-5, restart=20)
+    assert ir["resid_f64"] < 1e-11 and ir["outer"] >= 1
+    assert rel_err(xr, g["x"]) < 1e-9
 
 
 def test_stencils_standalone_bitexact(hz):
