@@ -450,18 +450,31 @@ int hz_build(hz_operator *op, int64_t *n_out)
         HZ_TRY(op->pos32.ensure(npad * sizeof(float4)));
         HZ_TRY(op->nrm32.ensure(npad * sizeof(float4)));
         HZ_TRY(op->tpos32.ensure(npad * sizeof(double4_32a)));
-        HZ_TRY(op->origin32.ensure((npad / kTile32) * sizeof(double4_32a)));
+        const int64_t ntiles = npad / kTile32;
+        op->r32.mwords = (ntiles + 31) / 32;
+        HZ_TRY(op->origin32.ensure(ntiles * sizeof(double4_32a)));
+        HZ_TRY(op->split32.ensure((2 * npad + 2 * ntiles) * sizeof(float4)));
+        HZ_TRY(op->nearmask32.ensure(ntiles * op->r32.mwords * sizeof(uint32_t)));
         HZ_TRY(op->dens32.ensure(npad * sizeof(float4)));
         HZ_TRY(sweep_order(N, n, op->idx.as<int64_t>(), op->perm.as<int>(), npad, op->scratch, s));
-        HZ_TRY(build_rec32(n, npad, op->perm.as<int>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
-                           op->pos32.as<float4>(), op->nrm32.as<float4>(), op->origin32.as<double4_32a>(),
-                           op->tpos32.as<double4_32a>(), sweep32_reg_scale(op->p.interior), s));
     }
     op->r32.perm = op->perm.as<int>();
     op->r32.pos = op->pos32.as<float4>();
     op->r32.nrm = op->nrm32.as<float4>();
     op->r32.origin = op->origin32.as<double4_32a>();
     op->r32.tpos = op->tpos32.as<double4_32a>();
+    {
+        float4 *sp = op->split32.as<float4>();
+        const int64_t ntiles = npad / kTile32;
+        op->r32.thi = sp;
+        op->r32.tlo = sp ? sp + npad : nullptr;
+        op->r32.ohi = sp ? sp + 2 * npad : nullptr;
+        op->r32.olo = sp ? sp + 2 * npad + ntiles : nullptr;
+        op->r32.nearmask = op->nearmask32.as<uint32_t>();
+    }
+    if (npad > 0)
+        HZ_TRY(build_rec32(op->r32, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
+                           sweep32_reg_scale(op->p.interior), op->tau, s));
     // scratch for the FP64 sweep densities (double4_32a per point) and staging
     HZ_TRY(op->scratch.ensure(nn * sizeof(double4_32a) + 256));
     HZ_TRY(op->io.ensure(nn * sizeof(double) * 8));

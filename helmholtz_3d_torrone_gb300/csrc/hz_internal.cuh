@@ -79,6 +79,17 @@ constexpr int kThreads64 = 128;
 
 // Sweep-order (spatially blocked) FP32 records.  perm[s] is the tube index
 // of sweep slot s; slots >= n are padding with zero weight.
+// Record a timing event on s.  Inside a stream capture the record becomes an
+// external event node (replayed with the graph); outside it is a plain record.
+inline cudaError_t record_timing_event(cudaEvent_t ev, cudaStream_t s)
+{
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    const cudaError_t e = cudaStreamIsCapturing(s, &st);
+    if (e != cudaSuccess) return e;
+    if (st == cudaStreamCaptureStatusActive) return cudaEventRecordWithFlags(ev, s, cudaEventRecordExternal);
+    return cudaEventRecord(ev, s);
+}
+
 struct Rec32 {
     int64_t npad;        // multiple of kTile32 and of kThreads32*kTgt32
     int *perm;           // npad entries, -1 for padding
@@ -86,6 +97,11 @@ struct Rec32 {
     float4 *nrm;         // nx, ny, nz, w
     double4_32a *origin;     // per tile: origin (x, y, z) and bounding radius .w
     double4_32a *tpos;       // per slot FP64 position (x, y, z), .w = w (targets)
+    float4 *thi, *tlo;       // per slot position split into FP32 head + tail (x = hi + lo)
+    float4 *ohi, *olo;       // per tile origin split into FP32 head + tail
+    uint32_t *nearmask;      // [target tile][mwords]: bit s set unless source tile s is
+                             // farther than tau from every point of the target tile
+    int64_t mwords;          // 32-bit words per mask row: ceil(tiles / 32)
 };
 
 struct SweepConst {
@@ -133,9 +149,11 @@ int sweep_order(int N, int64_t n, const int64_t *idx, int *perm, int64_t npad, D
                 cudaStream_t s);
 // reg_scale multiplies the regularisation factor stored in pos32.w (the
 // FP32 sweep folds sg/(4 pi) into its densities and divides it out here).
-int build_rec32(int64_t n, int64_t npad, const int *perm, const double4_32a *pos64,
-                const double4_32a *nrm64, float4 *pos32, float4 *nrm32, double4_32a *origin,
-                double4_32a *tpos, double reg_scale, cudaStream_t s);
+// Fill every array of r (npad, perm and the pointers set by the caller):
+// FP32 records, tile origins, split positions and the near-tile mask for
+// the regularisation radius tau.
+int build_rec32(const Rec32 &r, const double4_32a *pos64, const double4_32a *nrm64, double reg_scale, double tau,
+                cudaStream_t s);
 // sweep_f64.cu
 int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re, const double *p_im,
               const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
@@ -171,7 +189,7 @@ struct hz_operator {
     hz::DevBuf pos64, nrm64;
     // FP32 sweep records
     hz::Rec32 r32{};
-    hz::DevBuf perm, pos32, nrm32, origin32, tpos32;
+    hz::DevBuf perm, pos32, nrm32, origin32, tpos32, split32, nearmask32;
     // scratch and error word
     hz::DevBuf scratch, err;
     hz::DevBuf io;  // staging for host <-> device vectors

@@ -5,27 +5,31 @@
 // Precision design:
 //  * Sources are stored in a spatially blocked sweep order (8^3 node
 //    blocks), so a tile of kTile32 consecutive sources is compact.  Each
-//    tile has an FP64 origin o; sources hold FP32 offsets x_s - o and every
-//    target forms x_t - o in FP64 before rounding, so the difference
-//    x_t - x_s of close pairs is exact to FP32 relative precision.
+//    tile has an FP64 origin o; sources hold FP32 offsets x_s - o.  Targets
+//    and origins are held as FP32 head + tail pairs, and a target forms
+//    x_t - o = (t_hi - o_hi) + (t_lo - o_lo): the head difference is rounded
+//    to half an ulp of itself, so the offset of close pairs keeps FP32
+//    relative precision with no FP64 instruction in the tile loop.
 //  * The phase k*rho is reduced in revolutions with k/(2 pi) split into a
-//    12-bit head kh and a tail kl: f = fma(rho, kh, -rint(rho*kh)) +
-//    rho*kl is exact to ~2^-24 before sin/cos run on the SFU.
+//    head kh and a tail kl: f = fma(rho, kh, -nint(rho*kh)) + rho*kl is
+//    exact to ~2^-24 before sin/cos run on the SFU.
 //  * The near-field test rho <= tau is decided in FP64 (with the FP64
 //    sweep's own arithmetic) whenever the FP32 rho^2 lies within 1e-4 of
 //    tau^2, so FP32 and FP64 operators classify every pair alike.
-//  * Per tile the contributions are summed in FP32, across tiles in FP64.
+//  * Per tile the contributions are summed in FP32; across tiles into FP32
+//    head + tail pairs by TwoSum (about 48 significant bits).
 //
 // Throughput design: the kernel is bound by instruction issue on the FP32
-// pipe.  A source tile whose bounding sphere is farther than tau (with a
-// 1e-3 margin) from the bounding spheres of all of the block's targets
-// holds no near pair, and runs a loop without near-field tests or selects;
-// only the few tiles next to the block's targets take the full loop.  The
-// factor sg/(4 pi) is folded into the densities (and divided out of the
-// stored regularisation factors).  TMA bulk copies stage source tiles in
-// shared memory, double-buffered on mbarriers with bounded waits.  Block
-// shape and targets per thread come from a small table of compiled
-// variants; the autotuner times them on the operator's own data.
+// pipe, and GB300 runs FP64 at 1/64 of the FP32 rate, so the tile loop
+// holds no FP64 instruction at all.  A source tile whose bounding sphere is
+// farther than tau (with a 1e-3 margin) from the bounding spheres of all of
+// the block's target tiles holds no near pair; a bit mask built once per
+// tube in FP64 says which, and such tiles run a loop without near-field
+// tests or selects.  The factor sg/(4 pi) is folded into the densities (and
+// divided out of the stored regularisation factors).  TMA bulk copies stage
+// source tiles in shared memory, double-buffered on mbarriers with bounded
+// waits.  Block shape and targets per thread come from a small table of
+// compiled variants; the autotuner times them on the operator's own data.
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
 
@@ -35,18 +39,30 @@ namespace {
 constexpr double kPi = 3.14159265358979323846264338328;
 
 struct Args32 {
-    int64_t n, npad;
+    int64_t n, npad, mwords;
     float wave, kh, kl;
     float tau2, guard_lo, guard_hi;
-    double tau, tau_far;
+    double tau;
     const float4 *pos, *nrm, *dens;
-    const double4_32a *origin, *tpos;
+    const float4 *thi, *tlo, *ohi, *olo;
+    const uint32_t *nearmask;
+    const double4_32a *tpos;
     const int *perm;
     const double4_32a *pos64;  // tube order (for the near-field guard)
     const double *p_re, *p_im, *pt_re, *pt_im;
     double *q_re, *q_im, *qt_re, *qt_im;
     unsigned *err;
 };
+
+// hi + lo += f without rounding loss (Knuth's TwoSum; FP32 only).
+__device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float f)
+{
+    const float s = hi + f;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (f - bp);
+    hi = s;
+    lo += e;
+}
 
 // dens[s] = scale (w p, pt) at sweep slot s, FP32, scale = sg / (4 pi).
 __global__ void prep32_kernel(int64_t npad, const int *__restrict__ perm, const double4_32a *__restrict__ tpos,
@@ -74,11 +90,11 @@ __global__ void prep32_kernel(int64_t npad, const int *__restrict__ perm, const 
 
 // One source against TG targets; NEAR selects the loop with near-field
 // handling.  Accumulates into fA (A p) and fH (A^H pt).
-template <int MODE, bool DIR, int TG, bool NEAR>
+template <int MODE, bool DIR, int NT, int TG, bool NEAR>
 __device__ __forceinline__ void pair_block(const Args32 &a, const float4 s_p, const float4 s_n, const float4 s_d,
                                            const float3 (&rel)[TG], const float3 (&tn)[TG], const float (&treg)[TG],
-                                           const double4_32a (&tp)[TG], int64_t src_slot, float (&fAr)[TG],
-                                           float (&fAi)[TG], float (&fHr)[TG], float (&fHi)[TG])
+                                           int64_t tslot0, int64_t src_slot, float (&fAr)[TG], float (&fAi)[TG],
+                                           float (&fHr)[TG], float (&fHi)[TG])
 {
 #pragma unroll
     for (int g = 0; g < TG; g++) {
@@ -92,14 +108,16 @@ __device__ __forceinline__ void pair_block(const Args32 &a, const float4 s_p, co
                 const int c = a.perm[src_slot];
                 if (c >= 0) {
                     const double4_32a q = a.pos64[c];
-                    const double x1 = tp[g].x - q.x, x2 = tp[g].y - q.y, x3 = tp[g].z - q.z;
+                    const double4_32a tp = a.tpos[tslot0 + (int64_t)g * NT];
+                    const double x1 = tp.x - q.x, x2 = tp.y - q.y, x3 = tp.z - q.z;
                     near = !(sqrt(x1 * x1 + x2 * x2 + x3 * x3) > a.tau);
                 }
             }
         }
         const float rinv = rsqrtf(r2);
         const float rho = r2 * rinv;
-        const float nn = rintf(rho * a.kh);
+        // nearest integer to rho kh (|rho kh| < 2^22): add and remove 1.5 2^23
+        const float nn = fmaf(rho, a.kh, 12582912.f) - 12582912.f;
         float f = fmaf(rho, a.kh, -nn);
         f = fmaf(rho, a.kl, f);
         float S, C;
@@ -140,24 +158,22 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
     __shared__ alignas(8) uint64_t bar[2];
 
     const int64_t slot0 = (int64_t)blockIdx.x * NT * TG + threadIdx.x;
-    double4_32a tp[TG];
-    float3 tn[TG];
+    float3 th[TG], tl[TG], tn[TG];
     float treg[TG];
-    double accAr[TG], accAi[TG], accHr[TG], accHi[TG];
+    // cross-tile sums: FP32 head + tail (TwoSum), about 48 significant bits
+    float hAr[TG], lAr[TG], hAi[TG], lAi[TG], hHr[TG], lHr[TG], hHi[TG], lHi[TG];
 #pragma unroll
     for (int g = 0; g < TG; g++) {
         const int64_t s = slot0 + (int64_t)g * NT;
-        tp[g] = a.tpos[s];
-        const float4 nn = a.nrm[s];
+        const float4 h = a.thi[s], l = a.tlo[s], nn = a.nrm[s];
+        th[g] = make_float3(h.x, h.y, h.z);
+        tl[g] = make_float3(l.x, l.y, l.z);
         tn[g] = make_float3(nn.x, nn.y, nn.z);
         treg[g] = a.pos[s].w;
-        accAr[g] = accAi[g] = accHr[g] = accHi[g] = 0.0;
+        hAr[g] = lAr[g] = hAi[g] = lAi[g] = hHr[g] = lHr[g] = hHi[g] = lHi[g] = 0.f;
     }
-    // bounding spheres of the block's targets (block-uniform)
-    double4_32a tsph[NTT];
-    const int64_t ttile0 = ((int64_t)blockIdx.x * NT * TG) / TS;
-#pragma unroll
-    for (int k = 0; k < NTT; k++) tsph[k] = a.origin[ttile0 + k];
+    // rows of the near-tile mask for the block's target tiles
+    const uint32_t *mrow = a.nearmask + ((int64_t)blockIdx.x * NT * TG / TS) * a.mwords;
 
     const int64_t ntiles = a.npad / TS;
     if (threadIdx.x == 0) {
@@ -178,17 +194,18 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
     for (int64_t tile = 0; tile < ntiles; tile++) {
         const int buf = (int)(tile & 1);
         if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
-        const double4_32a o = a.origin[tile];
-        bool far = true;
+        uint32_t word = 0;
 #pragma unroll
-        for (int k = 0; k < NTT; k++) {
-            const double ex = o.x - tsph[k].x, ey = o.y - tsph[k].y, ez = o.z - tsph[k].z;
-            far = far && (sqrt(ex * ex + ey * ey + ez * ez) - o.w - tsph[k].w > a.tau_far);
-        }
+        for (int k = 0; k < NTT; k++) word |= __ldg(mrow + k * a.mwords + (tile >> 5));
+        const bool far = ((word >> (tile & 31)) & 1u) == 0;
+        // x_t - o: head difference (rounded once, to half an ulp of itself)
+        // plus the tails
+        const float4 oh = a.ohi[tile], ol = a.olo[tile];
         float3 rel[TG];
 #pragma unroll
         for (int g = 0; g < TG; g++)
-            rel[g] = make_float3((float)(tp[g].x - o.x), (float)(tp[g].y - o.y), (float)(tp[g].z - o.z));
+            rel[g] = make_float3((th[g].x - oh.x) + (tl[g].x - ol.x), (th[g].y - oh.y) + (tl[g].y - ol.y),
+                                 (th[g].z - oh.z) + (tl[g].z - ol.z));
         const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
@@ -204,20 +221,24 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
         if (far) {
 #pragma unroll 2
             for (int j = 0; j < TS; j++)
-                pair_block<MODE, DIR, TG, false>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, tp, base + j,
-                                                 fAr, fAi, fHr, fHi);
+                pair_block<MODE, DIR, NT, TG, false>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
+                                                     base + j, fAr, fAi, fHr, fHi);
         } else {
 #pragma unroll 2
             for (int j = 0; j < TS; j++)
-                pair_block<MODE, DIR, TG, true>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, tp, base + j,
-                                                fAr, fAi, fHr, fHi);
+                pair_block<MODE, DIR, NT, TG, true>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
+                                                    base + j, fAr, fAi, fHr, fHi);
         }
 #pragma unroll
         for (int g = 0; g < TG; g++) {
-            accAr[g] += fAr[g];
-            accAi[g] += fAi[g];
-            accHr[g] += fHr[g];
-            accHi[g] += fHi[g];
+            if (MODE & SWEEP_A) {
+                two_sum_acc(hAr[g], lAr[g], fAr[g]);
+                two_sum_acc(hAi[g], lAi[g], fAi[g]);
+            }
+            if (MODE & SWEEP_AH) {
+                two_sum_acc(hHr[g], lHr[g], fHr[g]);
+                two_sum_acc(hHi[g], lHi[g], fHi[g]);
+            }
         }
         __syncthreads();
     }
@@ -227,13 +248,14 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
         const int c = a.perm[s];
         if (c < 0) continue;
         if (MODE & SWEEP_A) {
-            if (!isfinite(accAr[g]) || !isfinite(accAi[g])) atomicOr(a.err, DEV_ERR_NONFINITE);
-            a.q_re[c] = accAr[g] + 0.5 * a.p_re[c];
-            a.q_im[c] = accAi[g] + 0.5 * a.p_im[c];
+            const double r = (double)hAr[g] + (double)lAr[g], i = (double)hAi[g] + (double)lAi[g];
+            if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
+            a.q_re[c] = r + 0.5 * a.p_re[c];
+            a.q_im[c] = i + 0.5 * a.p_im[c];
         }
         if (MODE & SWEEP_AH) {
-            const double w = tp[g].w;
-            const double r = w * accHr[g], i = w * accHi[g];
+            const double w = a.tpos[s].w;
+            const double r = w * ((double)hHr[g] + (double)lHr[g]), i = w * ((double)hHi[g] + (double)lHi[g]);
             if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
             a.qt_re[c] = r + 0.5 * a.pt_re[c];
             a.qt_im[c] = i + 0.5 * a.pt_im[c];
@@ -256,6 +278,12 @@ void launch_cfg(int cfg, const Args32 &a, cudaStream_t s)
         break;
     case 3:
         sweep32_kernel<MODE, DIR, 256, 1, 3><<<(unsigned)(a.npad / 256), 256, 0, s>>>(a);
+        break;
+    case 4:
+        sweep32_kernel<MODE, DIR, 256, 2, 3><<<(unsigned)(a.npad / 512), 256, 0, s>>>(a);
+        break;
+    case 5:
+        sweep32_kernel<MODE, DIR, 128, 2, 6><<<(unsigned)(a.npad / 256), 128, 0, s>>>(a);
         break;
     default:
         sweep32_kernel<MODE, DIR, 256, 2, 2><<<(unsigned)(a.npad / 512), 256, 0, s>>>(a);
@@ -286,7 +314,7 @@ void split_wave(double wave, float &kh, float &kl)
 
 double sweep32_reg_scale(int interior) { return ((interior == 1) ? -1.0 : 1.0) * (4.0 * kPi); }
 
-int sweep32_num_configs() { return 4; }
+int sweep32_num_configs() { return 6; }
 
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode, const double *p_re,
               const double *p_im, const double *pt_re, const double *pt_im, double *q_re, double *q_im,
@@ -313,26 +341,30 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.wave = (float)c.wave;
     split_wave(c.wave, a.kh, a.kl);
     a.tau = c.tau;
-    a.tau_far = c.tau * (1.0 + 1e-3);
+    a.mwords = r.mwords;
+    a.thi = r.thi;
+    a.tlo = r.tlo;
+    a.ohi = r.ohi;
+    a.olo = r.olo;
+    a.nearmask = r.nearmask;
     a.tau2 = (float)(c.tau * c.tau);
     a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
     a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
     a.pos = r.pos;
     a.nrm = r.nrm;
     a.dens = dens;
-    a.origin = r.origin;
     a.tpos = r.tpos;
     a.perm = r.perm;
     a.pos64 = pos64;
     a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
     a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
     a.err = c.err;
-    if (ev0) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev0, s, cudaEventRecordExternal));
+    if (ev0) HZ_CHECK_CUDA(record_timing_event(ev0, s));
     if (mode == SWEEP_PAIR) launch32<SWEEP_PAIR>(cfg, a, c.dirichlet != 0, s);
     else if (mode == SWEEP_A) launch32<SWEEP_A>(cfg, a, c.dirichlet != 0, s);
     else launch32<SWEEP_AH>(cfg, a, c.dirichlet != 0, s);
     HZ_CHECK_LAUNCH();
-    if (ev1) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev1, s, cudaEventRecordExternal));
+    if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
     return HZ_OK;
 }
 

@@ -241,12 +241,12 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
     a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
     a.err = c.err;
-    if (ev0) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev0, s, cudaEventRecordExternal));
+    if (ev0) HZ_CHECK_CUDA(record_timing_event(ev0, s));
     if (mode == SWEEP_PAIR) launch64<SWEEP_PAIR>(a, c.dirichlet != 0, s);
     else if (mode == SWEEP_A) launch64<SWEEP_A>(a, c.dirichlet != 0, s);
     else launch64<SWEEP_AH>(a, c.dirichlet != 0, s);
     HZ_CHECK_LAUNCH();
-    if (ev1) HZ_CHECK_CUDA(cudaEventRecordWithFlags(ev1, s, cudaEventRecordExternal));
+    if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
     return HZ_OK;
 }
 

@@ -324,6 +324,7 @@ __global__ void __launch_bounds__(kTile32) rec32_kernel(const int *__restrict__ 
                                                         const double4_32a *__restrict__ nrm64,
                                                         float4 *__restrict__ pos32, float4 *__restrict__ nrm32,
                                                         double4_32a *__restrict__ origin, double4_32a *__restrict__ tpos,
+                                                        float4 *__restrict__ thi, float4 *__restrict__ tlo,
                                                         double reg_scale)
 {
     const int64_t s = (int64_t)blockIdx.x * kTile32 + threadIdx.x;
@@ -374,7 +375,45 @@ __global__ void __launch_bounds__(kTile32) rec32_kernel(const int *__restrict__ 
         pos32[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         nrm32[s] = make_float4(0.f, 0.f, 0.f, 0.f);
         tpos[s] = make_double4_32a(org[0], org[1], org[2], 0.0);
+        p = make_double4_32a(org[0], org[1], org[2], 0.0);
     }
+    const float hx = (float)p.x, hy = (float)p.y, hz = (float)p.z;
+    thi[s] = make_float4(hx, hy, hz, 0.f);
+    tlo[s] = make_float4((float)(p.x - (double)hx), (float)(p.y - (double)hy), (float)(p.z - (double)hz), 0.f);
+}
+
+// Tile origins split into FP32 head + tail (x = hi + lo to about 2^-48 |x|).
+__global__ void split_origin_kernel(int64_t ntiles, const double4_32a *__restrict__ origin, float4 *__restrict__ ohi,
+                                    float4 *__restrict__ olo)
+{
+    const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (t >= ntiles) return;
+    const double4_32a o = origin[t];
+    const float hx = (float)o.x, hy = (float)o.y, hz = (float)o.z;
+    ohi[t] = make_float4(hx, hy, hz, 0.f);
+    olo[t] = make_float4((float)(o.x - (double)hx), (float)(o.y - (double)hy), (float)(o.z - (double)hz), 0.f);
+}
+
+// Near-tile mask: bit s of row t is clear only when the bounding spheres of
+// tiles t and s are more than tau_far apart, so that no pair between them
+// has rho <= tau (tau_far carries a 1e-3 relative margin).
+__global__ void nearmask_kernel(int64_t ntiles, int64_t mwords, const double4_32a *__restrict__ origin,
+                                double tau_far, uint32_t *__restrict__ mask)
+{
+    const int64_t id = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
+    if (id >= ntiles * mwords) return;
+    const int64_t t = id / mwords, w = id - t * mwords;
+    const double4_32a o = origin[t];
+    uint32_t bits = 0;
+    for (int b = 0; b < 32; b++) {
+        const int64_t q = w * 32 + b;
+        if (q >= ntiles) break;
+        const double4_32a u = origin[q];
+        const double ex = u.x - o.x, ey = u.y - o.y, ez = u.z - o.z;
+        const bool far = sqrt(ex * ex + ey * ey + ez * ez) - u.w - o.w > tau_far;
+        if (!far) bits |= 1u << b;
+    }
+    mask[id] = bits;
 }
 
 int grid_blocks(long long work, int threads)
@@ -449,13 +488,19 @@ int sweep_order(int N, int64_t n, const int64_t *idx, int *perm, int64_t npad, D
     return HZ_OK;
 }
 
-int build_rec32(int64_t n, int64_t npad, const int *perm, const double4_32a *pos64, const double4_32a *nrm64,
-                float4 *pos32, float4 *nrm32, double4_32a *origin, double4_32a *tpos, double reg_scale,
+int build_rec32(const Rec32 &r, const double4_32a *pos64, const double4_32a *nrm64, double reg_scale, double tau,
                 cudaStream_t s)
 {
-    (void)n;
-    rec32_kernel<<<(unsigned)(npad / kTile32), kTile32, 0, s>>>(perm, pos64, nrm64, pos32, nrm32, origin, tpos,
-                                                                 reg_scale);
+    const int64_t ntiles = r.npad / kTile32;
+    if (ntiles == 0) return HZ_OK;
+    rec32_kernel<<<(unsigned)ntiles, kTile32, 0, s>>>(r.perm, pos64, nrm64, r.pos, r.nrm, r.origin, r.tpos, r.thi,
+                                                      r.tlo, reg_scale);
+    HZ_CHECK_LAUNCH();
+    split_origin_kernel<<<(unsigned)((ntiles + 255) / 256), 256, 0, s>>>(ntiles, r.origin, r.ohi, r.olo);
+    HZ_CHECK_LAUNCH();
+    const int64_t cells = ntiles * r.mwords;
+    nearmask_kernel<<<(unsigned)((cells + 255) / 256), 256, 0, s>>>(ntiles, r.mwords, r.origin, tau * (1.0 + 1e-3),
+                                                                    r.nearmask);
     HZ_CHECK_LAUNCH();
     return HZ_OK;
 }

@@ -93,6 +93,32 @@ def test_matvec_f32_close_to_f64(hz, built, case):
     assert rel_err(qh2, g["AHp"]) < 2e-5
 
 
+def test_every_sweep_variant_and_autotune(hz, built):
+    """Each compiled FP32 sweep variant gives the reference's products to
+    FP32 accuracy; the autotuner (and timed products) run outside a graph."""
+    op, g, m = built["ref_dirichlet_torus_n32"]
+    cfg = 0
+    while True:
+        try:
+            op.set_sweep_config(cfg)
+        except hz.HzError:
+            break
+        q, qh = op.matvec_pair(g["p"], g["p"], precision=hz.PREC_F32)
+        assert rel_err(q, g["Ap"]) < 2e-5, cfg
+        assert rel_err(qh, g["AHp"]) < 2e-5, cfg
+        assert rel_err(op.matvec(g["p"], precision=hz.PREC_F32), g["Ap"]) < 2e-5, cfg
+        cfg += 1
+    assert cfg >= 4
+    best, ms = op.autotune()
+    assert 0 <= best < cfg and ms > 0
+    op.sweep_timing(1)
+    q = op.matvec(g["p"], precision=hz.PREC_F32)
+    t, k = op.sweep_timing(-1)
+    op.sweep_timing(0)
+    assert k >= 1 and t > 0
+    assert rel_err(q, g["Ap"]) < 2e-5
+
+
 @pytest.mark.parametrize("case", CASES)
 def test_bicg_f64_vs_reference_compbicg(hz, built, case):
     op, g, m = built[case]
