@@ -472,6 +472,12 @@ int hz_build(hz_operator *op, int64_t *n_out)
         op->r32.olo = sp ? sp + 2 * npad + ntiles : nullptr;
         op->r32.nearmask = op->nearmask32.as<uint32_t>();
     }
+    if (npad > 0) {
+        const size_t pb = sweep32_partial_bytes();
+        HZ_TRY(op->partial32.ensure(pb));
+        op->r32.partial = op->partial32.as<double4_32a>();
+        op->r32.partial_bytes = pb;
+    }
     if (npad > 0)
         HZ_TRY(build_rec32(op->r32, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
                            sweep32_reg_scale(op->p.interior), op->tau, s));

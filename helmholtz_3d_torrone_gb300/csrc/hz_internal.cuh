@@ -102,6 +102,8 @@ struct Rec32 {
     uint32_t *nearmask;      // [target tile][mwords]: bit s set unless source tile s is
                              // farther than tau from every point of the target tile
     int64_t mwords;          // 32-bit words per mask row: ceil(tiles / 32)
+    double4_32a *partial;    // stream-K scratch: pieces of target blocks split between CTAs
+    size_t partial_bytes;
 };
 
 struct SweepConst {
@@ -168,6 +170,8 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
 double sweep32_reg_scale(int interior);
 // number of compiled FP32 sweep variants (block shape x targets per thread)
 int sweep32_num_configs();
+// bytes of stream-K scratch that every FP32 sweep variant fits in
+size_t sweep32_partial_bytes();
 
 }  // namespace hz
 
@@ -189,7 +193,7 @@ struct hz_operator {
     hz::DevBuf pos64, nrm64;
     // FP32 sweep records
     hz::Rec32 r32{};
-    hz::DevBuf perm, pos32, nrm32, origin32, tpos32, split32, nearmask32;
+    hz::DevBuf perm, pos32, nrm32, origin32, tpos32, split32, nearmask32, partial32;
     // scratch and error word
     hz::DevBuf scratch, err;
     hz::DevBuf io;  // staging for host <-> device vectors

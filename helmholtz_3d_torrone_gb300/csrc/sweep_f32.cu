@@ -52,7 +52,19 @@ struct Args32 {
     const double *p_re, *p_im, *pt_re, *pt_im;
     double *q_re, *q_im, *qt_re, *qt_im;
     unsigned *err;
+    // stream-K partition: CTA c takes work units [c U / P, (c+1) U / P) of
+    // the U = blocks x tiles (target block, source tile) units
+    int64_t units;
+    int64_t nctas;
+    double4_32a *partial;  // [P][2][slots per block]: (A re, A im, A^H re, A^H im)
 };
+
+// The CTA whose unit range holds work unit u: the largest c with
+// floor(c U / P) <= u.
+__device__ __forceinline__ int64_t cta_of_unit(int64_t u, int64_t units, int64_t nctas)
+{
+    return ((u + 1) * nctas - 1) / units;
+}
 
 // hi + lo += f without rounding loss (Knuth's TwoSum; FP32 only).
 __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float f)
@@ -147,155 +159,244 @@ __device__ __forceinline__ void pair_block(const Args32 &a, const float4 s_p, co
     }
 }
 
+// Final value of one target slot: q = sum + p/2 (A), qt = w sum + pt/2 (A^H).
+template <int MODE>
+__device__ __forceinline__ void write_slot(const Args32 &a, int64_t s, double ar, double ai, double hr, double hi)
+{
+    const int c = a.perm[s];
+    if (c < 0) return;
+    if (MODE & SWEEP_A) {
+        if (!isfinite(ar) || !isfinite(ai)) atomicOr(a.err, DEV_ERR_NONFINITE);
+        a.q_re[c] = ar + 0.5 * a.p_re[c];
+        a.q_im[c] = ai + 0.5 * a.p_im[c];
+    }
+    if (MODE & SWEEP_AH) {
+        const double w = a.tpos[s].w;
+        const double r = w * hr, i = w * hi;
+        if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
+        a.qt_re[c] = r + 0.5 * a.pt_re[c];
+        a.qt_im[c] = i + 0.5 * a.pt_im[c];
+    }
+}
+
+// Persistent stream-K sweep: every CTA walks its own contiguous range of
+// (target block, source tile) units, so all CTAs carry the same number of
+// tile pairs whatever the tube size.  A target block that lies wholly in
+// one CTA's range is written out directly; the pieces of a block split
+// between CTAs go to the partial buffer (slot 0: the CTA's first block,
+// slot 1: its last) and sweep32_fixup adds them up in CTA order.
 template <int MODE, bool DIR, int NT, int TG, int MINB>
 __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
 {
     constexpr int TS = kTile32;
-    constexpr int NTT = (NT * TG + TS - 1) / TS;  // target tiles per block
+    constexpr int SLOTS = NT * TG;   // target slots per block (a multiple of TS)
+    constexpr int NTT = SLOTS / TS;  // target tiles per block
     __shared__ alignas(128) float4 sp[2][TS];
     __shared__ alignas(128) float4 sn[2][TS];
     __shared__ alignas(128) float4 sd[2][TS];
     __shared__ alignas(8) uint64_t bar[2];
 
-    const int64_t slot0 = (int64_t)blockIdx.x * NT * TG + threadIdx.x;
-    float3 th[TG], tl[TG], tn[TG];
-    float treg[TG];
-    // cross-tile sums: FP32 head + tail (TwoSum), about 48 significant bits
-    float hAr[TG], lAr[TG], hAi[TG], lAi[TG], hHr[TG], lHr[TG], hHi[TG], lHi[TG];
-#pragma unroll
-    for (int g = 0; g < TG; g++) {
-        const int64_t s = slot0 + (int64_t)g * NT;
-        const float4 h = a.thi[s], l = a.tlo[s], nn = a.nrm[s];
-        th[g] = make_float3(h.x, h.y, h.z);
-        tl[g] = make_float3(l.x, l.y, l.z);
-        tn[g] = make_float3(nn.x, nn.y, nn.z);
-        treg[g] = a.pos[s].w;
-        hAr[g] = lAr[g] = hAi[g] = lAi[g] = hHr[g] = lHr[g] = hHi[g] = lHi[g] = 0.f;
-    }
-    // rows of the near-tile mask for the block's target tiles
-    const uint32_t *mrow = a.nearmask + ((int64_t)blockIdx.x * NT * TG / TS) * a.mwords;
-
     const int64_t ntiles = a.npad / TS;
+    const int64_t u_begin = (int64_t)blockIdx.x * a.units / a.nctas;
+    const int64_t u_end = ((int64_t)blockIdx.x + 1) * a.units / a.nctas;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
         mbar_init(&bar[1], 1);
         fence_barrier_init();
     }
     __syncthreads();
-    auto issue = [&](int64_t tile, int buf) {
-        const int64_t base = tile * TS;
+    if (u_begin >= u_end) return;
+    auto issue = [&](int64_t u, int buf) {
+        const int64_t base = (u % ntiles) * TS;
         const uint32_t bytes = TS * sizeof(float4);
         mbar_arrive_expect_tx(&bar[buf], 3 * bytes);
         bulk_g2s(&sp[buf][0], a.pos + base, bytes, &bar[buf]);
         bulk_g2s(&sn[buf][0], a.nrm + base, bytes, &bar[buf]);
         bulk_g2s(&sd[buf][0], a.dens + base, bytes, &bar[buf]);
     };
-    if (threadIdx.x == 0) issue(0, 0);
-    for (int64_t tile = 0; tile < ntiles; tile++) {
-        const int buf = (int)(tile & 1);
-        if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
-        uint32_t word = 0;
+    if (threadIdx.x == 0) issue(u_begin, 0);
+    int seg = 0;
+    for (int64_t u = u_begin; u < u_end;) {
+        const int64_t blk = u / ntiles;
+        const int64_t seg_end = (u_end < (blk + 1) * ntiles) ? u_end : (blk + 1) * ntiles;
+        const bool whole = (u == blk * ntiles) && (seg_end == (blk + 1) * ntiles);
+        const int64_t slot0 = blk * SLOTS + threadIdx.x;
+        float3 th[TG], tl[TG], tn[TG];
+        float treg[TG];
+        // cross-tile sums: FP32 head + tail (TwoSum), about 48 significant bits
+        float hAr[TG], lAr[TG], hAi[TG], lAi[TG], hHr[TG], lHr[TG], hHi[TG], lHi[TG];
 #pragma unroll
-        for (int k = 0; k < NTT; k++) word |= __ldg(mrow + k * a.mwords + (tile >> 5));
-        const bool far = ((word >> (tile & 31)) & 1u) == 0;
-        // x_t - o: head difference (rounded once, to half an ulp of itself)
-        // plus the tails
-        const float4 oh = a.ohi[tile], ol = a.olo[tile];
-        float3 rel[TG];
-#pragma unroll
-        for (int g = 0; g < TG; g++)
-            rel[g] = make_float3((th[g].x - oh.x) + (tl[g].x - ol.x), (th[g].y - oh.y) + (tl[g].y - ol.y),
-                                 (th[g].z - oh.z) + (tl[g].z - ol.z));
-        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
-        if (__syncthreads_or(!ok)) {
-            if (threadIdx.x == 0) {
-                atomicOr(a.err, DEV_ERR_WAIT);
-                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
-            }
-            return;
+        for (int g = 0; g < TG; g++) {
+            const int64_t s = slot0 + (int64_t)g * NT;
+            const float4 h = a.thi[s], l = a.tlo[s], nn = a.nrm[s];
+            th[g] = make_float3(h.x, h.y, h.z);
+            tl[g] = make_float3(l.x, l.y, l.z);
+            tn[g] = make_float3(nn.x, nn.y, nn.z);
+            treg[g] = a.pos[s].w;
+            hAr[g] = lAr[g] = hAi[g] = lAi[g] = hHr[g] = lHr[g] = hHi[g] = lHi[g] = 0.f;
         }
-        float fAr[TG], fAi[TG], fHr[TG], fHi[TG];
+        // rows of the near-tile mask for this block's target tiles
+        const uint32_t *mrow = a.nearmask + (blk * NTT) * a.mwords;
+        for (; u < seg_end; u++) {
+            const int64_t it = u - u_begin;
+            const int buf = (int)(it & 1);
+            if (threadIdx.x == 0 && u + 1 < u_end) issue(u + 1, buf ^ 1);
+            const int64_t tile = u - blk * ntiles;
+            uint32_t word = 0;
 #pragma unroll
-        for (int g = 0; g < TG; g++) fAr[g] = fAi[g] = fHr[g] = fHi[g] = 0.f;
-        const int64_t base = tile * TS;
-        if (far) {
+            for (int k = 0; k < NTT; k++) word |= __ldg(mrow + k * a.mwords + (tile >> 5));
+            const bool far = ((word >> (tile & 31)) & 1u) == 0;
+            // x_t - o: head difference (rounded once, to half an ulp of
+            // itself) plus the tails
+            const float4 oh = a.ohi[tile], ol = a.olo[tile];
+            float3 rel[TG];
+#pragma unroll
+            for (int g = 0; g < TG; g++)
+                rel[g] = make_float3((th[g].x - oh.x) + (tl[g].x - ol.x), (th[g].y - oh.y) + (tl[g].y - ol.y),
+                                     (th[g].z - oh.z) + (tl[g].z - ol.z));
+            const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((it >> 1) & 1), kWaitLimit);
+            if (__syncthreads_or(!ok)) {
+                if (threadIdx.x == 0) {
+                    atomicOr(a.err, DEV_ERR_WAIT);
+                    if (u + 1 < u_end) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimit);
+                }
+                return;
+            }
+            float fAr[TG], fAi[TG], fHr[TG], fHi[TG];
+#pragma unroll
+            for (int g = 0; g < TG; g++) fAr[g] = fAi[g] = fHr[g] = fHi[g] = 0.f;
+            const int64_t base = tile * TS;
+            if (far) {
 #pragma unroll 2
-            for (int j = 0; j < TS; j++)
-                pair_block<MODE, DIR, NT, TG, false>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
-                                                     base + j, fAr, fAi, fHr, fHi);
-        } else {
+                for (int j = 0; j < TS; j++)
+                    pair_block<MODE, DIR, NT, TG, false>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
+                                                         base + j, fAr, fAi, fHr, fHi);
+            } else {
 #pragma unroll 2
-            for (int j = 0; j < TS; j++)
-                pair_block<MODE, DIR, NT, TG, true>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
-                                                    base + j, fAr, fAi, fHr, fHi);
+                for (int j = 0; j < TS; j++)
+                    pair_block<MODE, DIR, NT, TG, true>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
+                                                        base + j, fAr, fAi, fHr, fHi);
+            }
+#pragma unroll
+            for (int g = 0; g < TG; g++) {
+                if (MODE & SWEEP_A) {
+                    two_sum_acc(hAr[g], lAr[g], fAr[g]);
+                    two_sum_acc(hAi[g], lAi[g], fAi[g]);
+                }
+                if (MODE & SWEEP_AH) {
+                    two_sum_acc(hHr[g], lHr[g], fHr[g]);
+                    two_sum_acc(hHi[g], lHi[g], fHi[g]);
+                }
+            }
+            __syncthreads();
         }
 #pragma unroll
         for (int g = 0; g < TG; g++) {
-            if (MODE & SWEEP_A) {
-                two_sum_acc(hAr[g], lAr[g], fAr[g]);
-                two_sum_acc(hAi[g], lAi[g], fAi[g]);
+            const double ar = (double)hAr[g] + (double)lAr[g], ai = (double)hAi[g] + (double)lAi[g];
+            const double hr = (double)hHr[g] + (double)lHr[g], hi = (double)hHi[g] + (double)lHi[g];
+            if (whole) {
+                write_slot<MODE>(a, slot0 + (int64_t)g * NT, ar, ai, hr, hi);
+            } else {
+                a.partial[((int64_t)blockIdx.x * 2 + seg) * SLOTS + threadIdx.x + g * NT] =
+                    make_double4_32a(ar, ai, hr, hi);
             }
-            if (MODE & SWEEP_AH) {
-                two_sum_acc(hHr[g], lHr[g], fHr[g]);
-                two_sum_acc(hHi[g], lHi[g], fHi[g]);
-            }
         }
-        __syncthreads();
-    }
-#pragma unroll
-    for (int g = 0; g < TG; g++) {
-        const int64_t s = slot0 + (int64_t)g * NT;
-        const int c = a.perm[s];
-        if (c < 0) continue;
-        if (MODE & SWEEP_A) {
-            const double r = (double)hAr[g] + (double)lAr[g], i = (double)hAi[g] + (double)lAi[g];
-            if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
-            a.q_re[c] = r + 0.5 * a.p_re[c];
-            a.q_im[c] = i + 0.5 * a.p_im[c];
-        }
-        if (MODE & SWEEP_AH) {
-            const double w = a.tpos[s].w;
-            const double r = w * ((double)hHr[g] + (double)lHr[g]), i = w * ((double)hHi[g] + (double)lHi[g]);
-            if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
-            a.qt_re[c] = r + 0.5 * a.pt_re[c];
-            a.qt_im[c] = i + 0.5 * a.pt_im[c];
-        }
+        seg = 1;
     }
 }
 
-// Compiled variants: block size, targets per thread, minimum resident blocks.
-// Every variant covers 256 or 512 sweep slots per block (npad is a multiple
-// of 512).
-template <int MODE, bool DIR>
-void launch_cfg(int cfg, const Args32 &a, cudaStream_t s)
+// Adds up, in CTA order, the pieces of every target block that the stream-K
+// partition split between CTAs (one CTA per target block; blocks that one
+// CTA covered whole return at once).
+template <int MODE, int SLOTS>
+__global__ void __launch_bounds__(256) sweep32_fixup(Args32 a)
 {
-    switch (cfg) {
-    case 1:
-        sweep32_kernel<MODE, DIR, 128, 2, 4><<<(unsigned)(a.npad / 256), 128, 0, s>>>(a);
-        break;
-    case 2:
-        sweep32_kernel<MODE, DIR, 128, 4, 2><<<(unsigned)(a.npad / 512), 128, 0, s>>>(a);
-        break;
-    case 3:
-        sweep32_kernel<MODE, DIR, 256, 1, 3><<<(unsigned)(a.npad / 256), 256, 0, s>>>(a);
-        break;
-    case 4:
-        sweep32_kernel<MODE, DIR, 256, 2, 3><<<(unsigned)(a.npad / 512), 256, 0, s>>>(a);
-        break;
-    case 5:
-        sweep32_kernel<MODE, DIR, 128, 2, 6><<<(unsigned)(a.npad / 256), 128, 0, s>>>(a);
-        break;
-    default:
-        sweep32_kernel<MODE, DIR, 256, 2, 2><<<(unsigned)(a.npad / 512), 256, 0, s>>>(a);
-        break;
+    const int64_t blk = blockIdx.x;
+    const int64_t ntiles = a.npad / kTile32;
+    const int64_t c_lo = cta_of_unit(blk * ntiles, a.units, a.nctas);
+    const int64_t c_hi = cta_of_unit((blk + 1) * ntiles - 1, a.units, a.nctas);
+    if (c_lo == c_hi) return;
+    for (int k = threadIdx.x; k < SLOTS; k += blockDim.x) {
+        double ar = 0.0, ai = 0.0, hr = 0.0, hi = 0.0;
+        for (int64_t c = c_lo; c <= c_hi; c++) {
+            const int64_t first = (c * a.units / a.nctas) / ntiles;  // first block of CTA c
+            const int sg = (first == blk) ? 0 : 1;
+            const double4_32a v = a.partial[(c * 2 + sg) * SLOTS + k];
+            ar += v.x;
+            ai += v.y;
+            hr += v.z;
+            hi += v.w;
+        }
+        write_slot<MODE>(a, blk * SLOTS + k, ar, ai, hr, hi);
+    }
+}
+
+// Resident CTAs of one sweep instantiation on this device (cached).
+template <int MODE, bool DIR, int NT, int TG, int MINB>
+int64_t resident_ctas()
+{
+    static int64_t cached = 0;
+    if (cached == 0) {
+        int dev = 0, sms = 152, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep32_kernel<MODE, DIR, NT, TG, MINB>, NT, 0) !=
+                cudaSuccess ||
+            per < 1) {
+            cudaGetLastError();
+            per = MINB;
+        }
+        cached = (int64_t)per * sms;
+    }
+    return cached;
+}
+
+// persistent: one CTA per resident slot (stream-K); otherwise one CTA per
+// target block (the partition then never splits a block).
+template <int MODE, bool DIR, int NT, int TG, int MINB>
+int launch_streamk(Args32 a, bool persistent, size_t partial_bytes, cudaStream_t s)
+{
+    constexpr int SLOTS = NT * TG;
+    const int64_t blocks = a.npad / SLOTS;
+    a.units = blocks * (a.npad / kTile32);
+    int64_t p = persistent ? resident_ctas<MODE, DIR, NT, TG, MINB>() : blocks;
+    if (p > a.units) p = a.units;
+    if (persistent && (size_t)p * 2 * SLOTS * sizeof(double4_32a) > partial_bytes)
+        p = partial_bytes / (2 * SLOTS * sizeof(double4_32a));
+    if (p < 1) {
+        set_error("FP32 sweep: stream-K partial buffer too small");
+        return HZ_ERR_STATE;
+    }
+    a.nctas = p;
+    sweep32_kernel<MODE, DIR, NT, TG, MINB><<<(unsigned)p, NT, 0, s>>>(a);
+    HZ_CHECK_LAUNCH();
+    if (p != blocks) {
+        sweep32_fixup<MODE, SLOTS><<<(unsigned)blocks, 256, 0, s>>>(a);
+        HZ_CHECK_LAUNCH();
+    }
+    return HZ_OK;
+}
+
+// Compiled variants: (block size, targets per thread, minimum resident
+// blocks) x (persistent stream-K grid, or one CTA per target block).  Every
+// shape covers 256 or 512 sweep slots per block (npad is a multiple of 512).
+constexpr int kShapes = 4;
+template <int MODE, bool DIR>
+int launch_cfg(int cfg, const Args32 &a, size_t pb, cudaStream_t s)
+{
+    const bool persistent = cfg < kShapes;
+    switch (cfg % kShapes) {
+    case 1: return launch_streamk<MODE, DIR, 128, 2, 4>(a, persistent, pb, s);
+    case 2: return launch_streamk<MODE, DIR, 256, 1, 3>(a, persistent, pb, s);
+    case 3: return launch_streamk<MODE, DIR, 128, 2, 6>(a, persistent, pb, s);
+    default: return launch_streamk<MODE, DIR, 256, 2, 2>(a, persistent, pb, s);
     }
 }
 
 template <int MODE>
-void launch32(int cfg, const Args32 &a, bool dir, cudaStream_t s)
+int launch32(int cfg, const Args32 &a, bool dir, size_t pb, cudaStream_t s)
 {
-    if (dir) launch_cfg<MODE, true>(cfg, a, s);
-    else launch_cfg<MODE, false>(cfg, a, s);
+    return dir ? launch_cfg<MODE, true>(cfg, a, pb, s) : launch_cfg<MODE, false>(cfg, a, pb, s);
 }
 
 }  // namespace
@@ -314,7 +415,34 @@ void split_wave(double wave, float &kh, float &kl)
 
 double sweep32_reg_scale(int interior) { return ((interior == 1) ? -1.0 : 1.0) * (4.0 * kPi); }
 
-int sweep32_num_configs() { return 6; }
+int sweep32_num_configs() { return 2 * kShapes; }
+
+namespace {
+template <int MODE, bool DIR, int NT, int TG, int MINB>
+size_t partial_need()
+{
+    return (size_t)resident_ctas<MODE, DIR, NT, TG, MINB>() * 2 * NT * TG * sizeof(double4_32a);
+}
+template <int MODE, bool DIR>
+size_t partial_need_all()
+{
+    size_t m = 0;
+    const size_t v[kShapes] = {partial_need<MODE, DIR, 256, 2, 2>(), partial_need<MODE, DIR, 128, 2, 4>(),
+                               partial_need<MODE, DIR, 256, 1, 3>(), partial_need<MODE, DIR, 128, 2, 6>()};
+    for (size_t x : v) m = x > m ? x : m;
+    return m;
+}
+}  // namespace
+
+size_t sweep32_partial_bytes()
+{
+    const size_t v[6] = {partial_need_all<SWEEP_A, false>(),    partial_need_all<SWEEP_A, true>(),
+                         partial_need_all<SWEEP_AH, false>(),   partial_need_all<SWEEP_AH, true>(),
+                         partial_need_all<SWEEP_PAIR, false>(), partial_need_all<SWEEP_PAIR, true>()};
+    size_t m = 0;
+    for (size_t x : v) m = x > m ? x : m;
+    return m;
+}
 
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode, const double *p_re,
               const double *p_im, const double *pt_re, const double *pt_im, double *q_re, double *q_im,
@@ -360,10 +488,10 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
     a.err = c.err;
     if (ev0) HZ_CHECK_CUDA(record_timing_event(ev0, s));
-    if (mode == SWEEP_PAIR) launch32<SWEEP_PAIR>(cfg, a, c.dirichlet != 0, s);
-    else if (mode == SWEEP_A) launch32<SWEEP_A>(cfg, a, c.dirichlet != 0, s);
-    else launch32<SWEEP_AH>(cfg, a, c.dirichlet != 0, s);
-    HZ_CHECK_LAUNCH();
+    a.partial = r.partial;
+    if (mode == SWEEP_PAIR) HZ_TRY(launch32<SWEEP_PAIR>(cfg, a, c.dirichlet != 0, r.partial_bytes, s));
+    else if (mode == SWEEP_A) HZ_TRY(launch32<SWEEP_A>(cfg, a, c.dirichlet != 0, r.partial_bytes, s));
+    else HZ_TRY(launch32<SWEEP_AH>(cfg, a, c.dirichlet != 0, r.partial_bytes, s));
     if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
     return HZ_OK;
 }
