@@ -69,6 +69,8 @@ def parse():
     ap.add_argument("--method", choices=["bicg", "gmres"], nargs="*", default=["bicg", "gmres"],
                     help="--solve: inner Krylov method(s) of the refined solves")
     ap.add_argument("--restart", type=int, default=40, help="--solve: GMRES restart length")
+    ap.add_argument("--sweep-variant", type=int, default=-1,
+                    help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
 
 
@@ -198,7 +200,11 @@ def run_gb300(a, rank, world, local):
     op.set_stream(stream.cuda_stream)
     op.set_distance(d)
     n = op.build()
-    sweep_cfg, sweep_cfg_ms = op.autotune()  # untimed: picks the FP32 sweep variant for this tube
+    if a.sweep_variant >= 0:
+        op.set_sweep_config(a.sweep_variant)
+        sweep_cfg = a.sweep_variant
+    else:
+        sweep_cfg, sweep_cfg_ms = op.autotune()  # untimed: picks the FP32 sweep variant for this tube
     b = op.rhs_point_source(np.array([0.6, 0.0, 0.0]), hz.RHS_POINT_DIRICHLET)
     fp32_peak, fp64_peak = hz.measure_fma_peaks()
 

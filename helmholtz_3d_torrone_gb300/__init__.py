@@ -56,6 +56,21 @@ class SolveOpts(C.Structure):
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("stagnation", C.c_int), ("restart", C.c_int)]
 
 
+class DenseOpts(C.Structure):
+    """hz_dense_opts: switches and arguments of the dense assemblers."""
+    _fields_ = [("delta0", C.c_double), ("epsilon", C.c_double), ("wavenum", C.c_double), ("eta", C.c_double),
+                ("poly", C.c_int), ("sine", C.c_int), ("onesided", C.c_int), ("combo_interior", C.c_int),
+                ("radius", C.c_double), ("center", C.c_double * 3)]
+
+
+class RefConfig(C.Structure):
+    """hz_ref_config: the compile-time switches the reference-signature
+    dense assemblers read (include/helmholtz_ref_api.h)."""
+    _fields_ = [("int_l", C.c_double), ("int_u", C.c_double), ("tau_factor", C.c_double), ("interior", C.c_int),
+                ("poly", C.c_int), ("sine", C.c_int), ("trad_onesided", C.c_int), ("combo_onesided", C.c_int),
+                ("combo_interior", C.c_int), ("radius", C.c_double), ("center", C.c_double * 3)]
+
+
 class SolveInfo(C.Structure):
     _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("resid", C.c_double), ("resid_f64", C.c_double),
                 ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int)]
@@ -101,6 +116,13 @@ SIGNATURES = {
     "hz_reinitialize": ([C.c_int, C.c_double, _vp, C.c_int, C.c_double, C.c_int, C.c_int], C.c_int),
     "hz_dense_bicg": ([C.c_int64, _vp, _vp, _vp, _vp, _vp, _vp, C.c_double, C.c_int, C.c_int,
                        C.POINTER(SolveInfo)], C.c_int),
+    "hz_dense_opts_default": ([C.POINTER(DenseOpts), C.c_int, C.POINTER(Params)], None),
+    "hz_dense_count": ([C.c_int, C.POINTER(Params), C.POINTER(DenseOpts), _vp, C.c_int, C.POINTER(C.c_int64)],
+                       C.c_int),
+    "hz_dense_assemble": ([C.c_int, C.POINTER(Params), C.POINTER(DenseOpts)] + [_vp] * 6 +
+                          [C.c_int64] + [_vp] * 5 + [C.POINTER(C.c_int64), C.c_int], C.c_int),
+    "hz_ref_get_config": ([C.POINTER(RefConfig)], None),
+    "hz_ref_set_config": ([C.POINTER(RefConfig)], None),
     "hz_kernel_launches": ([], C.c_int64),
     "hz_measure_fma_peaks": ([_dp, _dp], C.c_int),
     "hz_eval_slice": ([_vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp,
@@ -377,6 +399,64 @@ def dense_bicg(A, b, tol=1e-7, maxit=1000):
     _check(load().hz_dense_bicg(n, _ptr(are), _ptr(aim), _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), tol, maxit,
                                 HZ_HOST, C.byref(info)))
     return xr + 1j * xi, info.as_dict()
+
+
+# ------------------------------------------------------------ dense assemblers
+DENSE_DOUBLE_LAYER, DENSE_COMBO, DENSE_SPHERE = 0, 1, 2
+DENSE_ROWS = ["zx", "zy", "zz", "xs", "ys", "zs", "dist", "gx", "gy", "gz", "delta", "jac", "curv", "reg",
+              "regimg", "polyw", "sinew", "polyres", "sineres", "result"]
+
+
+def dense_opts(kind, p, **kw):
+    """hz_dense_opts with the reference's defaults for kind, then kw."""
+    o = DenseOpts()
+    load().hz_dense_opts_default(C.byref(o), kind, C.byref(p))
+    for k, v in kw.items():
+        if k == "center":
+            o.center[:] = list(v)
+        else:
+            setattr(o, k, v)
+    return o
+
+
+def dense_assemble(kind, p, o, d=None, grids=None, matrices=True):
+    """Assemble one of the dense operators of HelmholtzKernel.c on the GPU.
+
+    Returns (pts [20][n], K1, K2, regcount): K1 the double-layer or PolyWeight
+    matrix, K2 the SineWeight matrix (None when not assembled)."""
+    L = load()
+    dd = None if d is None else _f64(d)
+    n = C.c_int64()
+    _check(L.hz_dense_count(kind, C.byref(p), C.byref(o), None if dd is None else _ptr(dd), HZ_HOST, C.byref(n)))
+    n = n.value
+    g = [None] * 5 if grids is None else [_f64(x) for x in grids]
+    pts = np.zeros((len(DENSE_ROWS), n))
+    want1 = matrices and (kind == DENSE_DOUBLE_LAYER or o.poly)
+    want2 = matrices and kind != DENSE_DOUBLE_LAYER and o.sine
+    m1 = [np.empty((n, n)), np.empty((n, n))] if want1 else [None, None]
+    m2 = [np.empty((n, n)), np.empty((n, n))] if want2 else [None, None]
+    rc = C.c_int64()
+    ptr = lambda a: None if a is None else _ptr(a)
+    _check(L.hz_dense_assemble(kind, C.byref(p), C.byref(o), ptr(dd), *[ptr(x) for x in g], n, _ptr(pts),
+                               ptr(m1[0]), ptr(m1[1]), ptr(m2[0]), ptr(m2[1]), C.byref(rc), HZ_HOST))
+    K1 = None if m1[0] is None else m1[0] + 1j * m1[1]
+    K2 = None if m2[0] is None else m2[0] + 1j * m2[1]
+    return pts, K1, K2, rc.value
+
+
+def ref_config(**kw):
+    """Read (and with kw, update) the switches of the reference-signature
+    dense assemblers; returns the configuration in force."""
+    c = RefConfig()
+    load().hz_ref_get_config(C.byref(c))
+    if kw:
+        for k, v in kw.items():
+            if k == "center":
+                c.center[:] = list(v)
+            else:
+                setattr(c, k, v)
+        load().hz_ref_set_config(C.byref(c))
+    return c
 
 
 # ------------------------------------------------------------------ text files

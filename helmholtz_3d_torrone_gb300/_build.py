@@ -22,6 +22,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "
 UNITS = {
     "stencils.cu": ["-fmad=false"],
     "tube.cu": ["-fmad=false"],
+    "dense.cu": ["-fmad=false"],
     "sweep_f64.cu": [],
     "sweep_f32.cu": [],
     "sweep_multi.cu": [],

@@ -201,6 +201,35 @@ struct MultiMatrixFreeOp final : MultiOp {
     }
 };
 
+// Copy count doubles in (host or device) to a device pointer.
+int stage_in(double *dst, const double *src, size_t count, int where, cudaStream_t s)
+{
+    if (!src) {
+        set_error("input pointer is NULL");
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                                  where == HZ_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
+    return HZ_OK;
+}
+
+int stage_out(double *dst, const double *src, size_t count, int where, cudaStream_t s)
+{
+    if (!dst) return HZ_OK;
+    HZ_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
+                                  where == HZ_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
+    return HZ_OK;
+}
+
+int where_ok(int where)
+{
+    if (where != HZ_HOST && where != HZ_DEVICE) {
+        set_error("where must be HZ_HOST or HZ_DEVICE");
+        return HZ_ERR_ARG;
+    }
+    return HZ_OK;
+}
+
 }  // namespace hz
 
 using namespace hz;
@@ -257,35 +286,6 @@ int need_built(hz_operator *op)
     if (!op->built) {
         set_error("hz_build has not been run");
         return HZ_ERR_STATE;
-    }
-    return HZ_OK;
-}
-
-// Copy count doubles in (host or device) to a device pointer.
-int stage_in(double *dst, const double *src, size_t count, int where, cudaStream_t s)
-{
-    if (!src) {
-        set_error("input pointer is NULL");
-        return HZ_ERR_ARG;
-    }
-    HZ_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
-                                  where == HZ_HOST ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToDevice, s));
-    return HZ_OK;
-}
-
-int stage_out(double *dst, const double *src, size_t count, int where, cudaStream_t s)
-{
-    if (!dst) return HZ_OK;
-    HZ_CHECK_CUDA(cudaMemcpyAsync(dst, src, count * sizeof(double),
-                                  where == HZ_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, s));
-    return HZ_OK;
-}
-
-int where_ok(int where)
-{
-    if (where != HZ_HOST && where != HZ_DEVICE) {
-        set_error("where must be HZ_HOST or HZ_DEVICE");
-        return HZ_ERR_ARG;
     }
     return HZ_OK;
 }

@@ -12,6 +12,12 @@ namespace hz {
 
 // ---------------------------------------------------------------- errors
 void set_error(const char *fmt, ...);
+// Host-or-device staging for the C ABI (capi.cu): copy count doubles from
+// src (host memory when where == HZ_HOST, device otherwise) to device dst,
+// and back; stage_out ignores a NULL dst.
+int stage_in(double *dst, const double *src, size_t count, int where, cudaStream_t s);
+int stage_out(double *dst, const double *src, size_t count, int where, cudaStream_t s);
+int where_ok(int where);
 void note_launch(int count = 1);
 
 #define HZ_CHECK_CUDA(call)                                                                      \
@@ -133,6 +139,14 @@ struct SweepTimer {
     void harvest(int count);
 };
 
+// dense.cu: the dense assemblers of HelmholtzKernel.c, all pointers on the
+// device (pts [HZ_DENSE_ROWS][n], matrices n x n row-major, may be NULL).
+int dense_assemble_device(int kind, const hz_params &p, const hz_dense_opts &o, const double *d, const double *gx,
+                          const double *gy, const double *gz, const double *mc, const double *gc, int64_t n_expected,
+                          double *pts, double *k1re, double *k1im, double *k2re, double *k2im,
+                          long long *regcount, unsigned *err, cudaStream_t s);
+int dense_count_device(int kind, const hz_params &p, const hz_dense_opts &o, const double *d, int64_t &n,
+                       cudaStream_t s);
 // stencils.cu
 int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
                          double *mc, double *gc, int order, cudaStream_t s);

@@ -119,3 +119,255 @@ int omp_CompBiCG(int size, double *density, double *densityimg, double **Kernel,
     // BICGSTAB.c:497 caps omp_CompBiCG at 2000 iterations
     return dense_bicg_ragged(size, density, densityimg, Kernel, Kernelimg, b, bimg, 2000);
 }
+
+// ---------------------------------------------------------------------------
+// Dense assemblers (HelmholtzKernel.c) with the reference's signatures.
+
+// The driver globals the reference's dense assemblers read
+// (HelmholtzKernel.h:16-18).  Weak definitions with the reference's initial
+// values (large3Dexample2.c:46-51): a driver that defines them, as
+// large3Dexample2.c does, supplies the values in use.
+__attribute__((weak, visibility("default"))) int N = 20;
+__attribute__((weak, visibility("default"))) int SIZE = 21;
+__attribute__((weak, visibility("default"))) double H = 0.0;
+__attribute__((weak, visibility("default"))) double HCUBED = 0.0;
+__attribute__((weak, visibility("default"))) double WAVE = 15.0;
+
+namespace {
+
+// frame.h / PDE.h values of the reference build
+hz_ref_config g_ref = {-2.0, 2.0, 2.0, 0, 0, 1, 0, 0, 0, 1.0, {0.0, 0.0, 0.0}};
+
+struct DeviceGrids {
+    hz::DevBuf buf;
+    const double *g[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+
+// hz_params of the driver's globals and the configuration; checks that the
+// driver's H is the configuration's (INT_U - INT_L)/N.
+int driver_params(hz_params &p, const char *who)
+{
+    if (N < 8 || SIZE != N + 1) {
+        hz::set_error("%s: driver globals N = %d, SIZE = %d are not set", who, N, SIZE);
+        return HZ_ERR_STATE;
+    }
+    hz_params_default(&p, N, WAVE);
+    p.int_l = g_ref.int_l;
+    p.int_u = g_ref.int_u;
+    p.tau_factor = g_ref.tau_factor;
+    p.interior = g_ref.interior;
+    const double h = (p.int_u - p.int_l) / p.N;
+    if (!(fabs(h - H) <= 1e-12 * h)) {
+        hz::set_error("%s: global H = %g differs from (INT_U - INT_L)/N = %g of the configuration", who, H, h);
+        return HZ_ERR_STATE;
+    }
+    return HZ_OK;
+}
+
+int upload_grids(double ***grids[6], int S, DeviceGrids &dg, const char *who)
+{
+    const size_t nodes = (size_t)S * S * S;
+    HZ_TRY(dg.buf.ensure(6 * nodes * sizeof(double)));
+    std::vector<double> tmp;
+    for (int q = 0; q < 6; q++) {
+        if (gather_grid(grids[q], S, tmp) != HZ_OK) {
+            hz::set_error("%s: ragged grid %d has NULL rows", who, q);
+            return HZ_ERR_ARG;
+        }
+        double *dst = dg.buf.as<double>() + q * nodes;
+        HZ_CHECK_CUDA(cudaMemcpy(dst, tmp.data(), nodes * sizeof(double), cudaMemcpyHostToDevice));
+        dg.g[q] = dst;
+    }
+    return HZ_OK;
+}
+
+// Copy one row of the per-point array (device) into a caller's list.
+int copy_row(double *dst, const double *dpts, int row, int64_t n)
+{
+    if (!dst || n == 0) return HZ_OK;
+    HZ_CHECK_CUDA(cudaMemcpy(dst, dpts + (size_t)row * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+    return HZ_OK;
+}
+
+// Copy a device n x n matrix into caller rows (one copy per row).
+int copy_rows(double **dst, const double *src, int64_t n, const char *who)
+{
+    if (!dst) return HZ_OK;
+    for (int64_t i = 0; i < n; i++) {
+        if (!dst[i]) {
+            hz::set_error("%s: NULL matrix row %lld", who, (long long)i);
+            return HZ_ERR_ARG;
+        }
+        HZ_CHECK_CUDA(cudaMemcpy(dst[i], src + (size_t)i * n, n * sizeof(double), cudaMemcpyDeviceToHost));
+    }
+    return HZ_OK;
+}
+
+// Assemble on the device: per-point rows into dpts, matrices into dm[0..3]
+// (k1 re/im, k2 re/im; NULL entries are not assembled).
+int run_dense(int kind, const hz_params &p, const hz_dense_opts &o, const DeviceGrids *dg, int64_t n,
+              hz::DevBuf &pbuf, hz::DevBuf &mbuf, double *dm[4], const bool want[4], long long *regcount)
+{
+    HZ_TRY(pbuf.ensure((size_t)HZ_DENSE_ROWS * (n > 0 ? n : 1) * sizeof(double)));
+    const size_t nn = (size_t)n * (size_t)n;
+    int cnt = 0;
+    for (int q = 0; q < 4; q++) cnt += want[q] ? 1 : 0;
+    HZ_TRY(mbuf.ensure((size_t)(cnt > 0 ? cnt : 1) * (nn > 0 ? nn : 1) * sizeof(double)));
+    int used = 0;
+    for (int q = 0; q < 4; q++) dm[q] = want[q] ? mbuf.as<double>() + (size_t)(used++) * nn : nullptr;
+    hz::DevBuf ebuf;
+    HZ_TRY(ebuf.ensure(sizeof(unsigned)));
+    HZ_CHECK_CUDA(cudaMemset(ebuf.ptr, 0, sizeof(unsigned)));
+    const double *g[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+    if (dg)
+        for (int q = 0; q < 6; q++) g[q] = dg->g[q];
+    HZ_TRY(hz::dense_assemble_device(kind, p, o, g[0], g[1], g[2], g[3], g[4], g[5], n, pbuf.as<double>(), dm[0],
+                                     dm[1], dm[2], dm[3], regcount, ebuf.as<unsigned>(), nullptr));
+    unsigned e = 0;
+    HZ_CHECK_CUDA(cudaMemcpy(&e, ebuf.ptr, sizeof(unsigned), cudaMemcpyDeviceToHost));
+    if (e & hz::DEV_ERR_GRID) {
+        hz::set_error("dense assembler: a projected point's interpolation cell lies outside the grid");
+        return HZ_ERR_GRID;
+    }
+    return HZ_OK;
+}
+
+}  // namespace
+
+extern "C" {
+void hz_ref_get_config(hz_ref_config *c)
+{
+    if (c) *c = g_ref;
+}
+void hz_ref_set_config(const hz_ref_config *c)
+{
+    if (c) g_ref = *c;
+}
+}
+
+int DoubleLayerKernel(int size, double epsilon, double ***level, double ***leveldx, double ***leveldy,
+                      double ***leveldz, double ***levelmcurv, double ***levelgcurv, double *zxlist, double *zylist,
+                      double *zzlist, double *zxstarlist, double *zystarlist, double *zzstarlist, double *dist,
+                      double *gradx, double *grady, double *gradz, double *delta, double *Jacobian, double *regfactor,
+                      double *regfactorimg, double *result, double **Kernel, double **Kernelimg, double wavenum)
+{
+    (void)wavenum;  // unused by the reference too (its kernel takes WAVE)
+    const char *who = "DoubleLayerKernel";
+    hz_params p;
+    HZ_TRY(driver_params(p, who));
+    hz_dense_opts o;
+    hz_dense_opts_default(&o, HZ_DENSE_DOUBLE_LAYER, &p);
+    o.epsilon = epsilon;
+    o.onesided = g_ref.trad_onesided;
+    DeviceGrids dg;
+    double ***grids[6] = {level, leveldx, leveldy, leveldz, levelmcurv, levelgcurv};
+    HZ_TRY(upload_grids(grids, SIZE, dg, who));
+    hz::DevBuf pbuf, mbuf;
+    double *dm[4];
+    const bool want[4] = {Kernel != nullptr, Kernelimg != nullptr, false, false};
+    HZ_TRY(run_dense(HZ_DENSE_DOUBLE_LAYER, p, o, &dg, size, pbuf, mbuf, dm, want, nullptr));
+    const double *P = pbuf.as<double>();
+    double *rows[15] = {zxlist, zylist, zzlist, zxstarlist, zystarlist, zzstarlist, dist, gradx, grady, gradz,
+                        delta, Jacobian, regfactor, regfactorimg, result};
+    const int idx[15] = {HZ_DP_ZX, HZ_DP_ZY, HZ_DP_ZZ, HZ_DP_XS, HZ_DP_YS, HZ_DP_ZS, HZ_DP_DIST, HZ_DP_GX,
+                         HZ_DP_GY, HZ_DP_GZ, HZ_DP_DELTA, HZ_DP_JAC, HZ_DP_REG, HZ_DP_REGIMG, HZ_DP_RESULT};
+    for (int q = 0; q < 15; q++) HZ_TRY(copy_row(rows[q], P, idx[q], size));
+    HZ_TRY(copy_rows(Kernel, dm[0], size, who));
+    HZ_TRY(copy_rows(Kernelimg, dm[1], size, who));
+    return 0;
+}
+
+int new_HelmholtzKernelCombo(int size, double delta, double epsilon, double ***level, double ***leveldx,
+                             double ***leveldy, double ***leveldz, double ***levelmcurv, double ***levelgcurv,
+                             double *zxlist, double *zylist, double *zzlist, double *zxstarlist, double *zystarlist,
+                             double *zzstarlist, double *dist, double *gradx, double *grady, double *gradz,
+                             double *Jacobian, double *regfactor, double *regfactorimg, double *PolyW, double *SineW,
+                             double *PolyResult, double *SineResult, double **PolyKernelH, double **PolyKernelHimg,
+                             double **SineKernelH, double **SineKernelHimg, double wavenum, double eta)
+{
+    const char *who = "new_HelmholtzKernelCombo";
+    hz_params p;
+    HZ_TRY(driver_params(p, who));
+    hz_dense_opts o;
+    hz_dense_opts_default(&o, HZ_DENSE_COMBO, &p);
+    o.delta0 = delta;
+    o.epsilon = epsilon;
+    o.wavenum = wavenum;
+    o.eta = eta;
+    o.poly = g_ref.poly;
+    o.sine = g_ref.sine;
+    o.onesided = g_ref.combo_onesided;
+    o.combo_interior = g_ref.combo_interior;
+    DeviceGrids dg;
+    double ***grids[6] = {level, leveldx, leveldy, leveldz, levelmcurv, levelgcurv};
+    HZ_TRY(upload_grids(grids, SIZE, dg, who));
+    hz::DevBuf pbuf, mbuf;
+    double *dm[4];
+    const bool want[4] = {o.poly && PolyKernelH, o.poly && PolyKernelHimg, o.sine && SineKernelH,
+                          o.sine && SineKernelHimg};
+    long long regcount = 0;
+    HZ_TRY(run_dense(HZ_DENSE_COMBO, p, o, &dg, size, pbuf, mbuf, dm, want, &regcount));
+    const double *P = pbuf.as<double>();
+    double *rows[13] = {zxlist, zylist, zzlist, zxstarlist, zystarlist, zzstarlist, dist, gradx, grady, gradz,
+                        Jacobian, regfactor, regfactorimg};
+    const int idx[13] = {HZ_DP_ZX, HZ_DP_ZY, HZ_DP_ZZ, HZ_DP_XS, HZ_DP_YS, HZ_DP_ZS, HZ_DP_DIST,
+                         HZ_DP_GX, HZ_DP_GY, HZ_DP_GZ, HZ_DP_JAC, HZ_DP_REG, HZ_DP_REGIMG};
+    for (int q = 0; q < 13; q++) HZ_TRY(copy_row(rows[q], P, idx[q], size));
+    if (o.poly) {
+        HZ_TRY(copy_row(PolyW, P, HZ_DP_POLYW, size));
+        HZ_TRY(copy_row(PolyResult, P, HZ_DP_POLYRES, size));
+        HZ_TRY(copy_rows(PolyKernelH, dm[0], size, who));
+        HZ_TRY(copy_rows(PolyKernelHimg, dm[1], size, who));
+    }
+    if (o.sine) {
+        HZ_TRY(copy_row(SineW, P, HZ_DP_SINEW, size));
+        HZ_TRY(copy_row(SineResult, P, HZ_DP_SINERES, size));
+        HZ_TRY(copy_rows(SineKernelH, dm[2], size, who));
+        HZ_TRY(copy_rows(SineKernelHimg, dm[3], size, who));
+    }
+    return (int)regcount;
+}
+
+int new_HelmholtzKernel(int size, double delta, double epsilon, double *zxlist, double *zylist, double *zzlist,
+                        double *zxstarlist, double *zystarlist, double *zzstarlist, double *dist, double *gradx,
+                        double *grady, double *gradz, double *curv, double *Jacobian, double *PolyW, double *SineW,
+                        double *PolyResult, double *SineResult, double **PolyKernelH, double **PolyKernelHimg,
+                        double **SineKernelH, double **SineKernelHimg)
+{
+    const char *who = "new_HelmholtzKernel";
+    hz_params p;
+    HZ_TRY(driver_params(p, who));
+    hz_dense_opts o;
+    hz_dense_opts_default(&o, HZ_DENSE_SPHERE, &p);
+    o.delta0 = delta;
+    o.epsilon = epsilon;
+    o.poly = g_ref.poly;
+    o.sine = g_ref.sine;
+    o.onesided = g_ref.combo_onesided;
+    o.radius = g_ref.radius;
+    for (int q = 0; q < 3; q++) o.center[q] = g_ref.center[q];
+    hz::DevBuf pbuf, mbuf;
+    double *dm[4];
+    const bool want[4] = {o.poly && PolyKernelH, o.poly && PolyKernelHimg, o.sine && SineKernelH,
+                          o.sine && SineKernelHimg};
+    HZ_TRY(run_dense(HZ_DENSE_SPHERE, p, o, nullptr, size, pbuf, mbuf, dm, want, nullptr));
+    const double *P = pbuf.as<double>();
+    double *rows[12] = {zxlist, zylist, zzlist, zxstarlist, zystarlist, zzstarlist, dist, gradx, grady, gradz,
+                        curv, Jacobian};
+    const int idx[12] = {HZ_DP_ZX, HZ_DP_ZY, HZ_DP_ZZ, HZ_DP_XS, HZ_DP_YS, HZ_DP_ZS,
+                         HZ_DP_DIST, HZ_DP_GX, HZ_DP_GY, HZ_DP_GZ, HZ_DP_CURV, HZ_DP_JAC};
+    for (int q = 0; q < 12; q++) HZ_TRY(copy_row(rows[q], P, idx[q], size));
+    if (o.poly) {
+        HZ_TRY(copy_row(PolyW, P, HZ_DP_POLYW, size));
+        HZ_TRY(copy_row(PolyResult, P, HZ_DP_POLYRES, size));
+        HZ_TRY(copy_rows(PolyKernelH, dm[0], size, who));
+        HZ_TRY(copy_rows(PolyKernelHimg, dm[1], size, who));
+    }
+    if (o.sine) {
+        HZ_TRY(copy_row(SineW, P, HZ_DP_SINEW, size));
+        HZ_TRY(copy_row(SineResult, P, HZ_DP_SINERES, size));
+        HZ_TRY(copy_rows(SineKernelH, dm[2], size, who));
+        HZ_TRY(copy_rows(SineKernelHimg, dm[3], size, who));
+    }
+    return 0;
+}

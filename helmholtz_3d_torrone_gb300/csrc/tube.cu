@@ -6,6 +6,7 @@
 // interpolate3D.c:5-102,569-605); only delta_eps (CUDA cos vs. the C
 // library's) can differ from the reference, by an ulp or so.
 #include "hz_internal.cuh"
+#include "interp.cuh"
 
 namespace hz {
 namespace {
@@ -168,17 +169,6 @@ int ordered_compaction(const Order &ord, long long total, const double *d, doubl
 }
 
 // ------------------------------------------------------- per-point arrays
-// interpolate3D.c:49-53 term order; letters are (x,y,z) = (j,i,k) low/high.
-__device__ __forceinline__ double tri8(double lll, double llh, double lhl, double lhh, double hll,
-                                       double hlh, double hhl, double hhh, double lx, double ly,
-                                       double lz, double H)
-{
-    return (lll * (H - lx) * (H - ly) * (H - lz) + llh * (H - lx) * (H - ly) * lz +
-            lhl * (H - lx) * ly * (H - lz) + lhh * (H - lx) * ly * lz + hll * lx * (H - ly) * (H - lz) +
-            hlh * lx * (H - ly) * lz + hhl * lx * ly * (H - lz) + hhh * lx * ly * lz) /
-           (H * H * H);
-}
-
 struct InitArgs {
     int N;
     double H, int_l, eps, tau, wave, HC;
@@ -212,30 +202,9 @@ __global__ void __launch_bounds__(256) init_kernel(InitArgs a)
         // :4392
         const double jac = 1 + 2. * dd * a.mc[o] + dd * dd * a.gc[o];
         // interpolate3D.c:21-29 cell of x*, then trilinear gradient (:41-77)
-        unsigned bad = 0;
-        int gi = (int)((ty - a.int_l) / H), gj = (int)((tx - a.int_l) / H), gk = (int)((tz - a.int_l) / H);
-        double lowx = tx - a.int_l - (double)(gj)*H;
-        double lowy = ty - a.int_l - (double)(gi)*H;
-        double lowz = tz - a.int_l - (double)(gk)*H;
-        if ((lowx > H) || (lowx < 0.0) || (lowy > H) || (lowy < 0.0) || (lowz < 0.0) || (lowz > H) ||
-            gi < 0 || gj < 0 || gk < 0 || gi >= a.N || gj >= a.N || gk >= a.N)
-            bad |= DEV_ERR_GRID;
         double nx = 0, ny = 0, nz = 0;
-        if (!bad) {
-            double r[3];
-            const double *g[3] = {a.gx, a.gy, a.gz};
-#pragma unroll
-            for (int cc = 0; cc < 3; cc++) {
-                const double *q = g[cc];
-                const long long b0 = (gi * S + gj) * S + gk;
-                r[cc] = tri8(q[b0], q[b0 + 1], q[b0 + S * S], q[b0 + S * S + 1], q[b0 + S], q[b0 + S + 1],
-                             q[b0 + S * S + S], q[b0 + S * S + S + 1], lowx, lowy, lowz, H);
-            }
-            const double nrm = sqrt(r[0] * r[0] + r[1] * r[1] + r[2] * r[2]);
-            nx = r[0] / nrm;
-            ny = r[1] / nrm;
-            nz = r[2] / nrm;
-            if (fabs(nrm - 1.0) > 0.5) bad |= DEV_ERR_NORMAL;
+        unsigned bad = interp_gradient(a.N, H, a.int_l, tx, ty, tz, a.gx, a.gy, a.gz, nx, ny, nz);
+        if (!(bad & DEV_ERR_GRID)) {
             // the driver normalises once more (:4408-4412)
             const double gn = sqrt(nx * nx + ny * ny + nz * nz);
             nx = nx / gn;
@@ -244,33 +213,7 @@ __global__ void __launch_bounds__(256) init_kernel(InitArgs a)
         }
         // interpolate3D.c:569-605 curvatures at x* (cell with a 1e-19 nudge)
         double cm = 0.0, cg = 0.0;
-        {
-            const int cj = (int)((tx + 1e-19 - a.int_l) / H);
-            const int ci = (int)((ty + 1e-19 - a.int_l) / H);
-            const int ck = (int)((tz + 1e-19 - a.int_l) / H);
-            if (ci < 0 || cj < 0 || ck < 0 || ci >= a.N || cj >= a.N || ck >= a.N) {
-                bad |= DEV_ERR_GRID;
-            } else {
-                const double lx = tx - a.int_l - (double)(cj)*H;
-                const double ly = ty - a.int_l - (double)(ci)*H;
-                const double lz = tz - a.int_l - (double)(ck)*H;
-                const double hc = H * H * H;
-                const long long b0 = (ci * S + cj) * S + ck;
-                const double *m2[2] = {a.mc, a.gc};
-                double r[2];
-#pragma unroll
-                for (int cc = 0; cc < 2; cc++) {
-                    const double *m = m2[cc];
-                    r[cc] = (m[b0] * (H - lx) * (H - ly) * (H - lz) + m[b0 + S * S] * (H - lx) * ly * (H - lz) +
-                             m[b0 + S] * lx * (H - ly) * (H - lz) + m[b0 + S * S + S] * lx * ly * (H - lz) +
-                             m[b0 + 1] * (H - lx) * (H - ly) * lz + m[b0 + S * S + 1] * (H - lx) * ly * lz +
-                             m[b0 + S + 1] * lx * (H - ly) * lz + m[b0 + S * S + S + 1] * lx * ly * lz) /
-                            hc;
-                }
-                cm = r[0];
-                cg = r[1];
-            }
-        }
+        bad |= interp_curvatures(a.N, H, a.int_l, tx, ty, tz, a.mc, a.gc, cm, cg);
         // :4427-4445 regularisation factor
         const double tau = a.tau;
         const double r1 = cm / (4. * PI * tau);

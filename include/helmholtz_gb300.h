@@ -239,6 +239,74 @@ HZ_API int hz_dense_bicg(int64_t n, const double *a_re, const double *a_im, cons
                   const double *b_im, double *x_re, double *x_im, double tol, int maxit,
                   int where, hz_solve_info *info);
 
+/* ---- Dense assemblers of HelmholtzKernel.c (small-n parity API) ----------
+ * The reference's dense n x n matrices, assembled on the device:
+ *   HZ_DENSE_DOUBLE_LAYER  DoubleLayerKernel        (HelmholtzKernel.c:613-761)
+ *   HZ_DENSE_COMBO         new_HelmholtzKernelCombo (HelmholtzKernel.c:173-610)
+ *   HZ_DENSE_SPHERE        new_HelmholtzKernel      (HelmholtzKernel.c:3-169),
+ *                          on the analytic sphere of hz_dense_opts
+ * Memory: two n x n FP64 matrices per assembled operator (3.2 GB each at
+ * n = 20,000); the matrix-free operator (hz_matvec) is the path at scale. */
+#define HZ_DENSE_DOUBLE_LAYER 0
+#define HZ_DENSE_COMBO 1
+#define HZ_DENSE_SPHERE 2
+
+/* Rows of the per-point array pts[HZ_DENSE_ROWS][n]; an assembler writes
+ * the rows its reference counterpart fills (the rest are left as they are). */
+enum {
+    HZ_DP_ZX, HZ_DP_ZY, HZ_DP_ZZ,    /* grid node                                 */
+    HZ_DP_XS, HZ_DP_YS, HZ_DP_ZS,    /* projection x*                              */
+    HZ_DP_DIST,                      /* signed distance at the node                */
+    HZ_DP_GX, HZ_DP_GY, HZ_DP_GZ,    /* unit normal at x*                          */
+    HZ_DP_DELTA,                     /* delta_eps (double layer)                   */
+    HZ_DP_JAC,                       /* Jacobian                                   */
+    HZ_DP_CURV,                      /* 1/(radius - d) (sphere kernel)             */
+    HZ_DP_REG, HZ_DP_REGIMG,         /* regularisation factor (double layer, Combo)*/
+    HZ_DP_POLYW, HZ_DP_SINEW,        /* annulus weights PolyWeight/SineWeight      */
+    HZ_DP_POLYRES, HZ_DP_SINERES,    /* H^3 J weight                               */
+    HZ_DP_RESULT,                    /* H^3 delta J (double layer)                 */
+    HZ_DENSE_ROWS
+};
+
+/* The reference's compile-time switches and call arguments of the dense
+ * assemblers (PDE.h, frame.h, functions.h).  hz_dense_opts_default gives the
+ * reference's values: POLY_TEST 0, SINE_TEST 1, one-sided switches 0, the
+ * frame.h sphere (radius 1 at the origin), eta = DEFAULT_ETA = -1, the
+ * driver's annulus [0.1 H, sqrt(H)] (large3Dexample2.c:61-63,298-305) and
+ * epsilon = FACTOR H for the double layer. */
+typedef struct hz_dense_opts {
+    double delta0;      /* inner radius of the annulus (Combo, sphere kernel)        */
+    double epsilon;     /* outer radius: |d| <= epsilon                               */
+    double wavenum;     /* Combo: wave number of the double-layer part (the single-
+                           layer part and the other assemblers use hz_params.wave)    */
+    double eta;         /* Combo: weight of the -i eta single-layer part              */
+    int poly, sine;     /* assemble the PolyWeight / SineWeight matrices              */
+    int onesided;       /* TRAD_ONESIDED (double layer) or COMBO_ONESIDED             */
+    int combo_interior; /* COMBO_INTERIOR                                              */
+    double radius;      /* analytic sphere of new_HelmholtzKernel (frame.h)           */
+    double center[3];
+} hz_dense_opts;
+
+HZ_API void hz_dense_opts_default(hz_dense_opts *o, int kind, const hz_params *p);
+
+/* Number of points the assembler selects from the distance grid d
+ * ((N+1)^3, ignored by HZ_DENSE_SPHERE, may then be NULL). */
+HZ_API int hz_dense_count(int kind, const hz_params *p, const hz_dense_opts *o, const double *d, int where,
+                          int64_t *n);
+
+/* Assemble.  d and the grids gx, gy, gz (WENO gradient), mc, gc (mean and
+ * Gaussian curvature) are (N+1)^3; pass NULL grids to have them computed
+ * from d on the device (hz_assign_gradient / hz_assign_curvatures).  n must
+ * equal hz_dense_count (HZ_ERR_ARG otherwise, where the reference exits).
+ * Outputs (any may be NULL): pts [HZ_DENSE_ROWS][n]; k1 = the double-layer
+ * matrix, or the PolyWeight matrix of Combo / sphere kernel; k2 = their
+ * SineWeight matrix; row-major n x n, real and imaginary parts.  regcount
+ * (may be NULL) receives the Combo's count of regularised pairs. */
+HZ_API int hz_dense_assemble(int kind, const hz_params *p, const hz_dense_opts *o, const double *d,
+                             const double *gx, const double *gy, const double *gz, const double *mc,
+                             const double *gc, int64_t n, double *pts, double *k1_re, double *k1_im,
+                             double *k2_re, double *k2_im, int64_t *regcount, int where);
+
 /* Number of kernel launches made by this library in this process (graph
  * launches count their kernels), for launch accounting. */
 HZ_API int64_t hz_kernel_launches(void);

@@ -38,4 +38,68 @@ HZ_API int CompBiCG(int size, double *density, double *densityimg, double **Kern
 HZ_API int omp_CompBiCG(int size, double *density, double *densityimg, double **Kernel, double **Kernelimg,
                         double *b, double *bimg, int chunk);
 
+/* ---- Dense assemblers (HelmholtzKernel.h:20-40) ------------------------
+ * Same arguments and outputs as the reference: per-point lists of length
+ * size and caller-owned ragged size x size matrices.  Like the reference
+ * they read the driver's globals N, SIZE, H, HCUBED, WAVE
+ * (HelmholtzKernel.h:16-18; defined by the driver, large3Dexample2.c:46-51)
+ * and its compile-time switches, which here are the runtime values of
+ * hz_ref_config (defaults: the reference headers' values).  size must equal
+ * the number of points the assembler selects (HZ_ERR_ARG otherwise; the
+ * reference exits).  The matrices are built on the device and copied row by
+ * row into the caller's arrays. */
+
+/* HelmholtzKernel.c:613-761: tube |d| <= epsilon, finite-difference double
+ * layer, regularised within TAU_FACTOR H; returns 0. */
+HZ_API int DoubleLayerKernel(int size, double epsilon, double ***level, double ***leveldx, double ***leveldy,
+                             double ***leveldz, double ***levelmcurv, double ***levelgcurv, double *zxlist,
+                             double *zylist, double *zzlist, double *zxstarlist, double *zystarlist,
+                             double *zzstarlist, double *dist, double *gradx, double *grady, double *gradz,
+                             double *delta, double *Jacobian, double *regfactor, double *regfactorimg,
+                             double *result, double **Kernel, double **Kernelimg, double wavenum);
+
+/* HelmholtzKernel.c:173-610: annulus delta <= |d| <= epsilon, -i eta single
+ * layer plus the hypersingular double layer at x*_i + |d_j| n_i; the
+ * PolyWeight / SineWeight matrices of the switches; returns regcount. */
+HZ_API int new_HelmholtzKernelCombo(int size, double delta, double epsilon, double ***level, double ***leveldx,
+                                    double ***leveldy, double ***leveldz, double ***levelmcurv,
+                                    double ***levelgcurv, double *zxlist, double *zylist, double *zzlist,
+                                    double *zxstarlist, double *zystarlist, double *zzstarlist, double *dist,
+                                    double *gradx, double *grady, double *gradz, double *Jacobian,
+                                    double *regfactor, double *regfactorimg, double *PolyW, double *SineW,
+                                    double *PolyResult, double *SineResult, double **PolyKernelH,
+                                    double **PolyKernelHimg, double **SineKernelH, double **SineKernelHimg,
+                                    double wavenum, double eta);
+
+/* HelmholtzKernel.c:3-169: the analytic sphere of the configuration
+ * (frame.h radius, Cx, Cy, Cz); returns 0. */
+HZ_API int new_HelmholtzKernel(int size, double delta, double epsilon, double *zxlist, double *zylist,
+                               double *zzlist, double *zxstarlist, double *zystarlist, double *zzstarlist,
+                               double *dist, double *gradx, double *grady, double *gradz, double *curv,
+                               double *Jacobian, double *PolyW, double *SineW, double *PolyResult,
+                               double *SineResult, double **PolyKernelH, double **PolyKernelHimg,
+                               double **SineKernelH, double **SineKernelHimg);
+
+/* The reference's compile-time switches read by the drop-ins above. */
+typedef struct hz_ref_config {
+    double int_l, int_u;     /* frame.h INT_L, INT_U            (-2, 2) */
+    double tau_factor;       /* PDE.h TAU_FACTOR                    (2) */
+    int interior;            /* PDE.h INTERIOR_MODE                 (0) */
+    int poly, sine;          /* PDE.h POLY_TEST, SINE_TEST       (0, 1) */
+    int trad_onesided;       /* PDE.h TRAD_ONESIDED                 (0) */
+    int combo_onesided;      /* PDE.h COMBO_ONESIDED                (0) */
+    int combo_interior;      /* PDE.h COMBO_INTERIOR                (0) */
+    double radius;           /* frame.h radius                      (1) */
+    double center[3];        /* frame.h Cx, Cy, Cz            (0, 0, 0) */
+} hz_ref_config;
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+HZ_API void hz_ref_get_config(hz_ref_config *c);
+HZ_API void hz_ref_set_config(const hz_ref_config *c);
+#ifdef __cplusplus
+}
+#endif
+
 #endif

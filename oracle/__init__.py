@@ -58,6 +58,19 @@ def make_params(N, wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, diri
     return Params(N, int_l, int_u, wave, factor, tau_factor, dirichlet, interior)
 
 
+class DenseOpts(C.Structure):
+    """Options of the dense assemblers (or_dense_opts)."""
+    _fields_ = [("delta0", C.c_double), ("epsilon", C.c_double), ("wavenum", C.c_double), ("eta", C.c_double),
+                ("poly", C.c_int), ("sine", C.c_int), ("onesided", C.c_int), ("combo_interior", C.c_int),
+                ("radius", C.c_double), ("cx", C.c_double), ("cy", C.c_double), ("cz", C.c_double)]
+
+
+# rows of the per-point arrays of the dense assemblers (or_dense_points)
+DENSE_ROWS = ["zx", "zy", "zz", "xs", "ys", "zs", "dist", "gx", "gy", "gz", "delta", "jac", "curv", "reg",
+              "regimg", "polyw", "sinew", "polyres", "sineres", "result"]
+DENSE_DOUBLE_LAYER, DENSE_COMBO, DENSE_SPHERE = 0, 1, 2
+
+
 class Oracle:
     """ctypes wrapper over ibim_oracle.c (every call is FP64 on the CPU)."""
 
@@ -87,6 +100,15 @@ class Oracle:
                               C.c_int, C.c_int]
         L.or_point_source_rhs.argtypes = [P, C.c_int64, _dp, _dp, _dp, C.c_int, _dp, _dp]
         L.or_reinit.argtypes = [C.c_int, C.c_double, _dp, C.c_int, C.c_double, C.c_int]
+        D = C.POINTER(DenseOpts)
+        L.or_dense_points.argtypes = [C.c_int, P, D] + [_dp] * 6 + [C.c_int64, _dp]
+        L.or_dense_points.restype = C.c_int64
+        L.or_dense_matrix.argtypes = [C.c_int, P, D, C.c_int64, _dp, _dp, _dp, _dp, _dp]
+        L.or_dense_matrix.restype = C.c_int64
+        L.or_poly_weight.argtypes = [C.c_double, C.c_double]
+        L.or_poly_weight.restype = C.c_double
+        L.or_sine_weight.argtypes = [C.c_double, C.c_double]
+        L.or_sine_weight.restype = C.c_double
 
     def weno(self, fi, dx, order=5):
         fi = np.ascontiguousarray(fi, dtype=np.float64)
@@ -186,6 +208,35 @@ class Oracle:
         self.L.or_point_source_rhs(C.byref(p), n, _d(tp["xs"]), _d(tp["nrm"]), _d(s), kind, _d(br), _d(bi))
         return br + 1j * bi
 
+    def dense_points(self, kind, p, o, d=None, grids=None):
+        """Per-point arrays of a dense assembler: dict of DENSE_ROWS."""
+        if grids is None:
+            args = [None] * 6 if d is None else [_d(np.ascontiguousarray(d))] + [None] * 5
+        else:
+            args = [_d(np.ascontiguousarray(d))] + [_d(np.ascontiguousarray(g)) for g in grids]
+        n = self.L.or_dense_points(kind, C.byref(p), C.byref(o), *args, 0, None)
+        if n < 0:
+            raise ValueError("interpolation cell outside the grid at point %d" % (-n - 1))
+        pts = np.zeros((len(DENSE_ROWS), n))
+        self.L.or_dense_points(kind, C.byref(p), C.byref(o), *args, n, _d(pts))
+        return {k: pts[i] for i, k in enumerate(DENSE_ROWS)}, pts
+
+    def dense_matrix(self, kind, p, o, pts):
+        """(K1, K2, regcount): K1 the double-layer or PolyWeight matrix, K2 the
+        SineWeight matrix (None when not assembled)."""
+        n = pts.shape[1]
+        pts = np.ascontiguousarray(pts)
+        k1 = [np.zeros((n, n)), np.zeros((n, n))]
+        k2 = [np.zeros((n, n)), np.zeros((n, n))] if kind != DENSE_DOUBLE_LAYER and o.sine else [None, None]
+        if kind != DENSE_DOUBLE_LAYER and not o.poly:
+            k1 = [None, None]
+        ptr = lambda a: None if a is None else _d(a)
+        rc = self.L.or_dense_matrix(kind, C.byref(p), C.byref(o), n, _d(pts), ptr(k1[0]), ptr(k1[1]),
+                                    ptr(k2[0]), ptr(k2[1]))
+        K1 = None if k1[0] is None else k1[0] + 1j * k1[1]
+        K2 = None if k2[0] is None else k2[0] + 1j * k2[1]
+        return K1, K2, int(rc)
+
     def pipeline(self, p, d):
         """Grids -> tube -> per-point arrays, all on the CPU."""
         N, H = p.N, p.H
@@ -220,7 +271,12 @@ class Reference:
         L.ref_dense_rows.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int]
         L.ref_compbicg.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
         L.ref_rows_matvec.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
-        L.ref_double_layer.argtypes = [C.c_int, _dp, _dp, _dp]
+        L.ref_double_layer.argtypes = [C.c_int, C.c_double, _dp, _dp, _dp]
+        L.ref_combo.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double] + [_dp] * 5
+        L.ref_combo.restype = C.c_int
+        L.ref_sphere_kernel.argtypes = [C.c_int, C.c_double, C.c_double] + [_dp] * 5
+        L.ref_dense_flags.argtypes = [_i32p]
+        L.ref_sphere.argtypes = [_dp]
         cfg = np.zeros(6)
         L.ref_config(_d(cfg))
         self.int_l, self.int_u, self.factor, self.tau_factor = cfg[:4]
@@ -275,13 +331,40 @@ class Reference:
         self.L.ref_dense_rows(n, r0, r1, _d(are), _d(aim), nthreads)
         return are, aim
 
-    def double_layer(self, n):
-        """DoubleLayerKernel: (per-point arrays dict, dense complex matrix)."""
-        pts = np.zeros((16, n))
+    def dense_flags(self):
+        """POLY_TEST, SINE_TEST, TRAD_ONESIDED, COMBO_ONESIDED, COMBO_INTERIOR,
+        INTERIOR_MODE of this build, and its frame.h sphere (radius, centre)."""
+        f = np.zeros(6, dtype=np.int32)
+        self.L.ref_dense_flags(f.ctypes.data_as(_i32p))
+        sph = np.zeros(4)
+        self.L.ref_sphere(_d(sph))
+        return dict(poly=int(f[0]), sine=int(f[1]), trad_onesided=int(f[2]), combo_onesided=int(f[3]),
+                    combo_interior=int(f[4]), interior=int(f[5]), radius=sph[0], center=tuple(sph[1:]))
+
+    def double_layer(self, n, epsilon=None):
+        """DoubleLayerKernel: (per-point rows (20 x n), dense complex matrix)."""
+        epsilon = self.ref_eps() if epsilon is None else epsilon
+        pts = np.zeros((20, n))
         are, aim = np.empty((n, n)), np.empty((n, n))
-        self.L.ref_double_layer(n, _d(pts), _d(are), _d(aim))
-        keys = ["zx", "zy", "zz", "xs", "ys", "zs", "dist", "gx", "gy", "gz", "delta", "jac", "reg", "regimg", "result"]
-        return {k: pts[i] for i, k in enumerate(keys)}, are + 1j * aim
+        self.L.ref_double_layer(n, epsilon, _d(pts), _d(are), _d(aim))
+        return pts, are + 1j * aim
+
+    def ref_eps(self):
+        return self.L.ref_eps()
+
+    def combo(self, n, delta0, epsilon, wavenum, eta):
+        """new_HelmholtzKernelCombo: (rows (20 x n), PolyK, SineK, regcount)."""
+        pts = np.zeros((20, n))
+        m = [np.zeros((n, n)) for _ in range(4)]
+        rc = self.L.ref_combo(n, delta0, epsilon, wavenum, eta, _d(pts), *[_d(a) for a in m])
+        return pts, m[0] + 1j * m[1], m[2] + 1j * m[3], rc
+
+    def sphere_kernel(self, n, delta0, epsilon):
+        """new_HelmholtzKernel on the frame.h sphere: (rows, PolyK, SineK)."""
+        pts = np.zeros((20, n))
+        m = [np.zeros((n, n)) for _ in range(4)]
+        self.L.ref_sphere_kernel(n, delta0, epsilon, _d(pts), *[_d(a) for a in m])
+        return pts, m[0] + 1j * m[1], m[2] + 1j * m[3]
 
     def rows_matvec(self, n, v, r0, r1, nthreads=os.cpu_count() or 1):
         vr = np.ascontiguousarray(v.real)

@@ -843,3 +843,327 @@ void or_point_source_rhs(const or_params *p, int64_t n, const double *xs, const 
         }
     }
 }
+
+/* ------------------------------------------------------------------ */
+/* Dense assemblers (HelmholtzKernel.c)                                */
+/* ------------------------------------------------------------------ */
+/* functions.h:25-26 (MOMENT_ORDER 1 constants of SineWeight) */
+#define OR_CONSTA1 -759.2781934172483
+#define OR_CONSTB1 446.2604260472818
+
+/* functions.c:793-833: first moment with smooth ends */
+double or_poly_weight(double t, double tau)
+{
+    if ((t <= tau) || (t >= 1.0)) return 0.0;
+    double tau2 = tau * tau;
+    double term1 = 7. * (1 + tau) * t;
+    double term2 = -2. * (2. + 3. * tau + 2. * tau2);
+    return 60. * (t - 1.) * (t - 1.) * (t - tau) * (t - tau) * (term1 + term2) / pow(tau - 1., 7.0);
+}
+
+/* functions.c:835-866, MOMENT_ORDER 1 */
+double or_sine_weight(double t, double tau)
+{
+    if ((t <= tau) || (t >= 1.0)) return 0.0;
+    return exp(0.5 / ((t - 0.1) * (t - 1.))) * (OR_CONSTA1 * t + OR_CONSTB1);
+}
+
+/* functions.c:433-456 (cal_phi, LAPLACE 0) */
+static double fd_phi_re(double wave, double xi, double yi, double zi, double xj, double yj, double zj)
+{
+    double norm = sqrt(fabs((xi - xj) * (xi - xj) + (yi - yj) * (yi - yj) + (zi - zj) * (zi - zj)));
+    if (norm == 0.0) return 0.0;
+    return cos(wave * norm) / (-4.0 * OR_PI * norm);
+}
+
+/* functions.c:481-504 (phiimg) */
+static double fd_phi_im(double wave, double xi, double yi, double zi, double xj, double yj, double zj)
+{
+    double norm = sqrt(fabs(pow(xi - xj, 2.0) + pow(yi - yj, 2.0) + pow(zi - zj, 2.0)));
+    if (norm == 0.0) return 0.0;
+    return sin(wave * norm) / (-4.0 * OR_PI * norm);
+}
+
+/* functions.c:121-155 (cal_partial): central difference of the fundamental
+ * solution in the second variable, step H; modes 1-3 real, 4-6 imaginary. */
+static void fd_partials(double H, double wave, const double *a, const double *b, double re[3], double im[3])
+{
+    re[0] = (fd_phi_re(wave, a[0], a[1], a[2], b[0] + H, b[1], b[2]) -
+             fd_phi_re(wave, a[0], a[1], a[2], b[0] - H, b[1], b[2])) / (2.0 * H);
+    re[1] = (fd_phi_re(wave, a[0], a[1], a[2], b[0], b[1] + H, b[2]) -
+             fd_phi_re(wave, a[0], a[1], a[2], b[0], b[1] - H, b[2])) / (2.0 * H);
+    re[2] = (fd_phi_re(wave, a[0], a[1], a[2], b[0], b[1], b[2] + H) -
+             fd_phi_re(wave, a[0], a[1], a[2], b[0], b[1], b[2] - H)) / (2.0 * H);
+    im[0] = (fd_phi_im(wave, a[0], a[1], a[2], b[0] + H, b[1], b[2]) -
+             fd_phi_im(wave, a[0], a[1], a[2], b[0] - H, b[1], b[2])) / (2.0 * H);
+    im[1] = (fd_phi_im(wave, a[0], a[1], a[2], b[0], b[1] + H, b[2]) -
+             fd_phi_im(wave, a[0], a[1], a[2], b[0], b[1] - H, b[2])) / (2.0 * H);
+    im[2] = (fd_phi_im(wave, a[0], a[1], a[2], b[0], b[1], b[2] + H) -
+             fd_phi_im(wave, a[0], a[1], a[2], b[0], b[1], b[2] - H)) / (2.0 * H);
+}
+
+/* Is node value d in the point set of the assembler? */
+static int dense_member(int kind, const or_dense_opts *o, double d)
+{
+    if (kind == OR_DENSE_DOUBLE_LAYER) { /* HelmholtzKernel.c:653-662 */
+        if (o->onesided == 0) return !(fabs(d) > o->epsilon);
+        return !((d > o->epsilon) || (d < 0.));
+    }
+    if (kind == OR_DENSE_COMBO) { /* :247-265 */
+        if (o->onesided == 0) return !((fabs(d) > o->epsilon) || (fabs(d) < o->delta0));
+        if (o->combo_interior == 1) return !((d > o->epsilon) || (d < o->delta0));
+        return !((d < -1. * o->epsilon) || (d > -1. * o->delta0));
+    }
+    /* :46-55 */
+    if (o->onesided == 0) return !((fabs(d) > o->epsilon) || (fabs(d) < o->delta0));
+    return !((d > o->epsilon) | (d < o->delta0));
+}
+
+static void dense_weights(const or_dense_opts *o, double hcubed, double dist, double jac, double *row, int64_t n,
+                          int64_t c)
+{
+    const double eps = o->epsilon;
+    if (o->poly) {
+        double w = (o->onesided == 0) ? or_poly_weight(fabs(dist / eps), o->delta0 / eps) / (2.0 * eps)
+                                      : or_poly_weight(fabs(dist / eps), o->delta0 / eps) / (eps);
+        row[OR_DP_POLYW * n + c] = w;
+        row[OR_DP_POLYRES * n + c] = hcubed * jac * w;
+    }
+    if (o->sine) {
+        double w = (o->onesided == 0) ? or_sine_weight(fabs(dist / eps), o->delta0 / eps) / (2.0 * eps)
+                                      : or_sine_weight(fabs(dist / eps), o->delta0 / eps) / (eps);
+        row[OR_DP_SINEW * n + c] = w;
+        row[OR_DP_SINERES * n + c] = hcubed * jac * w;
+    }
+}
+
+int64_t or_dense_points(int kind, const or_params *p, const or_dense_opts *o, const double *d,
+                        const double *gx, const double *gy, const double *gz, const double *mcurv,
+                        const double *gcurv, int64_t n_alloc, double *pts)
+{
+    const int N = p->N, S = N + 1;
+    const double H = or_h(p), hcubed = H * H * H, int_l = p->int_l, W = p->wave;
+    int64_t count = 0;
+    for (int i = 0; i < S; i++) {
+        const double zy = int_l + H * (double)(i);
+        for (int j = 0; j < S; j++) {
+            const double zx = int_l + H * (double)(j);
+            for (int k = 0; k < S; k++) {
+                const double zz = int_l + H * (double)(k);
+                double dd;
+                if (kind == OR_DENSE_SPHERE)
+                    dd = o->radius - sqrt((zx - o->cx) * (zx - o->cx) + (zy - o->cy) * (zy - o->cy) +
+                                          (zz - o->cz) * (zz - o->cz));
+                else
+                    dd = d[IDX(i, j, k)];
+                if (!dense_member(kind, o, dd)) continue;
+                const int64_t c = count++;
+                if (!pts || n_alloc <= 0) continue;
+                if (c >= n_alloc) continue;
+                const int64_t n = n_alloc;
+                double *row = pts;
+                row[OR_DP_ZX * n + c] = zx;
+                row[OR_DP_ZY * n + c] = zy;
+                row[OR_DP_ZZ * n + c] = zz;
+                row[OR_DP_DIST * n + c] = dd;
+                if (kind == OR_DENSE_SPHERE) {
+                    /* :57-98 */
+                    const double r0 = sqrt((zx - o->cx) * (zx - o->cx) + (zy - o->cy) * (zy - o->cy) +
+                                           (zz - o->cz) * (zz - o->cz));
+                    const double tgx = (o->cx - zx) / r0, tgy = (o->cy - zy) / r0, tgz = (o->cz - zz) / r0;
+                    const double sx = zx - dd * tgx, sy = zy - dd * tgy, sz = zz - dd * tgz;
+                    const double r1 = sqrt((sx - o->cx) * (sx - o->cx) + (sy - o->cy) * (sy - o->cy) +
+                                           (sz - o->cz) * (sz - o->cz));
+                    row[OR_DP_XS * n + c] = sx;
+                    row[OR_DP_YS * n + c] = sy;
+                    row[OR_DP_ZS * n + c] = sz;
+                    row[OR_DP_GX * n + c] = (o->cx - sx) / r1;
+                    row[OR_DP_GY * n + c] = (o->cy - sy) / r1;
+                    row[OR_DP_GZ * n + c] = (o->cz - sz) / r1;
+                    const double curv = 1. / (o->radius - dd);
+                    const double jac = 1. + dd * curv;
+                    row[OR_DP_CURV * n + c] = curv;
+                    row[OR_DP_JAC * n + c] = jac;
+                    dense_weights(o, hcubed, dd, jac, row, n, c);
+                    continue;
+                }
+                const size_t q = IDX(i, j, k);
+                const double sx = zx - dd * gx[q], sy = zy - dd * gy[q], sz = zz - dd * gz[q];
+                row[OR_DP_XS * n + c] = sx;
+                row[OR_DP_YS * n + c] = sy;
+                row[OR_DP_ZS * n + c] = sz;
+                double nx, ny, nz, cm, cg;
+                if (interp_grad(N, H, int_l, sx, sy, sz, gx, gy, gz, &nx, &ny, &nz) < 0) return -(1 + c);
+                if (kind == OR_DENSE_COMBO) { /* :299-303 second normalisation */
+                    double gn = sqrt(nx * nx + ny * ny + nz * nz);
+                    nx = nx / gn;
+                    ny = ny / gn;
+                    nz = nz / gn;
+                }
+                row[OR_DP_GX * n + c] = nx;
+                row[OR_DP_GY * n + c] = ny;
+                row[OR_DP_GZ * n + c] = nz;
+                const double jac = 1 + 2. * dd * mcurv[q] + dd * dd * gcurv[q];
+                row[OR_DP_JAC * n + c] = jac;
+                if (interp_curv(N, H, int_l, sx, sy, sz, mcurv, gcurv, &cm, &cg) < 0) return -(1 + c);
+                const double tau = H * p->tau_factor;
+                const double t1 = cm / (4. * OR_PI * tau);
+                const double t2 = -5. * tau * (2. * cm) * (4. * cm * cm - cg) / (512. * OR_PI);
+                const double t3 = -25. * tau * (2. * cm) * cg / (1536. * OR_PI);
+                const double t4 = W * W * tau * 2. * cm / (48. * OR_PI);
+                if (kind == OR_DENSE_DOUBLE_LAYER) { /* :700-725 */
+                    const double delta = (o->onesided == 0) ? cal_delta(o->epsilon, dd)
+                                                            : 2. * cal_delta(o->epsilon, dd);
+                    row[OR_DP_DELTA * n + c] = delta;
+                    row[OR_DP_REG * n + c] = t1 + t2 + t3 + t4;
+                    row[OR_DP_REGIMG * n + c] = 0.0;
+                    row[OR_DP_RESULT * n + c] = hcubed * delta * jac;
+                } else { /* :350-385 */
+                    row[OR_DP_REG * n + c] = (p->interior == 1) ? t1 + t2 + t3 + t4 : -1. * (t1 + t2 + t3 + t4);
+                    row[OR_DP_REGIMG * n + c] = 0.0;
+                    dense_weights(o, hcubed, dd, jac, row, n, c);
+                }
+            }
+        }
+    }
+    return count;
+}
+
+int64_t or_dense_matrix(int kind, const or_params *p, const or_dense_opts *o, int64_t n, const double *pts,
+                        double *k1re, double *k1im, double *k2re, double *k2im)
+{
+    const double H = or_h(p), W = p->wave;
+    const double *xs = pts + OR_DP_XS * n, *ys = pts + OR_DP_YS * n, *zs = pts + OR_DP_ZS * n;
+    const double *gx = pts + OR_DP_GX * n, *gy = pts + OR_DP_GY * n, *gz = pts + OR_DP_GZ * n;
+    const double *reg = pts + OR_DP_REG * n, *dist = pts + OR_DP_DIST * n;
+    const double *pres = pts + OR_DP_POLYRES * n, *sres = pts + OR_DP_SINERES * n, *res = pts + OR_DP_RESULT * n;
+    int64_t regcount = 0;
+    if (kind == OR_DENSE_DOUBLE_LAYER || kind == OR_DENSE_SPHERE) {
+        /* :726-758 and :125-166: finite-difference kernel gradients */
+        const double tau = (kind == OR_DENSE_DOUBLE_LAYER) ? H * p->tau_factor : 0.1 * H;
+        const double threshold = (kind == OR_DENSE_DOUBLE_LAYER) ? tau * tau : 0.01 * H * H;
+        double sreg = 0.0;
+        if (kind == OR_DENSE_SPHERE) { /* :19-32 */
+            const double R = o->radius;
+            const double r1 = 1.0 / (4.0 * OR_PI * tau * R);
+            const double r2 = (-5.0 * tau) / (256.0 * pow(R, 3.0) * OR_PI);
+            const double r3 = (-50.0 * tau) / (1536.0 * pow(R, 3.0) * OR_PI);
+            const double r4 = (pow(W, 2.0) * tau) / (24.0 * OR_PI * R);
+            sreg = (p->interior == 1) ? r1 + r2 + r3 + r4 : -1.0 * (r1 + r2 + r3 + r4);
+        }
+#pragma omp parallel for schedule(static)
+        for (int64_t i = 0; i < n; i++) {
+            const double a[3] = {xs[i], ys[i], zs[i]};
+            for (int64_t j = 0; j < n; j++) {
+                const double b[3] = {xs[j], ys[j], zs[j]};
+                double pr[3], pi[3];
+                fd_partials(H, W, a, b, pr, pi);
+                double part, parti;
+                const double n2 = (a[0] - b[0]) * (a[0] - b[0]) + (a[1] - b[1]) * (a[1] - b[1]) +
+                                  (a[2] - b[2]) * (a[2] - b[2]);
+                if (kind == OR_DENSE_DOUBLE_LAYER) {
+                    part = pr[0] * gx[i] + pr[1] * gy[i] + pr[2] * gz[i];
+                    parti = pi[0] * gx[i] + pi[1] * gy[i] + pi[2] * gz[i];
+                    if (n2 < threshold) {
+                        part = reg[i];
+                        parti = 0.0;
+                    }
+                    k1re[i * n + j] = res[j] * part;
+                    k1im[i * n + j] = res[j] * parti;
+                    if (i == j) k1re[i * n + j] += 0.5;
+                } else {
+                    part = -1. * (pr[0] * gx[i] + pr[1] * gy[i] + pr[2] * gz[i]);
+                    parti = -1. * (pi[0] * gx[i] + pi[1] * gy[i] + pi[2] * gz[i]);
+                    if (n2 < threshold) {
+                        part = sreg;
+                        parti = 0.0;
+                    }
+                    if (o->poly && k1re) {
+                        k1re[i * n + j] = part * pres[j];
+                        k1im[i * n + j] = parti * pres[j];
+                        if (i == j) k1re[i * n + j] -= 0.5;
+                    }
+                    if (o->sine && k2re) {
+                        k2re[i * n + j] = part * sres[j];
+                        k2im[i * n + j] = parti * sres[j];
+                        if (i == j) k2re[i * n + j] -= 0.5;
+                    }
+                }
+            }
+        }
+        return 0;
+    }
+    /* Combo, :399-607 */
+    const double tau = p->tau_factor * H;
+    const double recipfourpi = 1. / (4. * OR_PI);
+    const double k = o->wavenum, eta = o->eta;
+#pragma omp parallel for schedule(static) reduction(+ : regcount)
+    for (int64_t i = 0; i < n; i++) {
+        const double sxi = xs[i], syi = ys[i], szi = zs[i];
+        for (int64_t j = 0; j < n; j++) {
+            const double sxj = xs[j], syj = ys[j], szj = zs[j];
+            const double m1 = sxi - sxj, m2 = syi - syj, m3 = szi - szj;
+            const double mn = sqrt(m1 * m1 + m2 * m2 + m3 * m3);
+            double part, parti;
+            if (mn > tau) {
+                const double rn = 1. / mn;
+                const double prm = W * mn;
+                const double sv = sin(prm), cv = cos(prm);
+                const double es = sv * rn, ec = cv * rn;
+                const double den = recipfourpi * rn * rn;
+                const double c1 = -1. * (W * sv + ec) * den;
+                const double c2 = (W * cv - es) * den;
+                const double sip = -1. * (m1 * gx[i] + m2 * gy[i] + m3 * gz[i]);
+                part = c1 * sip;
+                parti = c2 * sip;
+            } else {
+                regcount += 1;
+                part = reg[i];
+                parti = 0.0;
+            }
+            double psr = 0, psi = 0, ssr = 0, ssi = 0;
+            if (o->poly) {
+                double tr = part * pres[j], ti = parti * pres[j];
+                if (i == j) tr -= 0.5;
+                psr = eta * ti;
+                psi = -1. * eta * tr;
+            }
+            if (o->sine) {
+                double tr = part * sres[j], ti = parti * sres[j];
+                if (i == j) tr -= 0.5;
+                ssr = eta * ti;
+                ssi = -1. * eta * tr;
+            }
+            const double x1 = sxi + fabs(dist[j]) * gx[i];
+            const double x2 = syi + fabs(dist[j]) * gy[i];
+            const double x3 = szi + fabs(dist[j]) * gz[i];
+            const double y1 = x1 - sxj, y2 = x2 - syj, y3 = x3 - szj;
+            const double yn = sqrt(y1 * y1 + y2 * y2 + y3 * y3);
+            const double rn = 1. / yn;
+            const double prm = k * yn;
+            const double ip1 = gx[i] * gx[j] + gy[i] * gy[j] + gz[i] * gz[j];
+            const double ip2 = y1 * gx[i] + y2 * gy[i] + y3 * gz[i];
+            const double ip3 = y1 * gx[j] + y2 * gy[j] + y3 * gz[j];
+            const double cm1 = ip1 * rn;
+            const double cm2 = ip2 * rn * ip3 * rn;
+            const double cv = cos(prm) * rn, sv = sin(prm) * rn;
+            const double t1r = -1. * (cv * rn + k * sv) * cm1;
+            const double t1i = (k * cv - sv * rn) * cm1;
+            const double t2r = -1. * k * k * cv * cm2;
+            const double t2i = -1. * k * k * sv * cm2;
+            const double t3r = 3. * k * sv * cm2 * rn;
+            const double t3i = -3. * k * cv * cm2 * rn;
+            const double t4r = 3. * cv * rn * cm2 * rn;
+            const double t4i = 3. * sv * rn * cm2 * rn;
+            if (o->poly && k1re) {
+                k1re[i * n + j] = psr + pres[j] * (t1r + t2r + t3r + t4r) * recipfourpi;
+                k1im[i * n + j] = psi + pres[j] * (t1i + t2i + t3i + t4i) * recipfourpi;
+            }
+            if (o->sine && k2re) {
+                k2re[i * n + j] = ssr + sres[j] * (t1r + t2r + t3r + t4r) * recipfourpi;
+                k2im[i * n + j] = ssi + sres[j] * (t1i + t2i + t3i + t4i) * recipfourpi;
+            }
+        }
+    }
+    return regcount;
+}

@@ -125,6 +125,54 @@ void or_eval(const or_params *p, int64_t n, const double *xs, const double *nrm,
 void or_point_source_rhs(const or_params *p, int64_t n, const double *xs, const double *nrm,
                          const double *src, int kind, double *bre, double *bim);
 
+/* ------------------------------------------------------------------ */
+/* Dense assemblers of HelmholtzKernel.c (small-n parity API)          */
+/* ------------------------------------------------------------------ */
+/* Options of the dense assemblers: the reference's compile-time switches
+ * (PDE.h POLY_TEST, SINE_TEST, TRAD_/COMBO_ONESIDED, COMBO_INTERIOR; the
+ * sphere of frame.h) and the arguments of the calls. */
+typedef struct {
+    double delta0;      /* inner radius of the annulus delta0 <= |d|        */
+    double epsilon;     /* outer radius |d| <= epsilon                       */
+    double wavenum;     /* Combo: wave number of the double-layer part       */
+    double eta;         /* Combo: coupling of the -i eta single-layer part   */
+    int poly, sine;     /* POLY_TEST / SINE_TEST                             */
+    int onesided;       /* TRAD_ONESIDED (double layer) / COMBO_ONESIDED     */
+    int combo_interior; /* COMBO_INTERIOR                                    */
+    double radius, cx, cy, cz; /* analytic sphere of new_HelmholtzKernel     */
+} or_dense_opts;
+
+/* Rows of the per-point output array pts[OR_DP_ROWS][n]. */
+enum {
+    OR_DP_ZX, OR_DP_ZY, OR_DP_ZZ, OR_DP_XS, OR_DP_YS, OR_DP_ZS, OR_DP_DIST, OR_DP_GX, OR_DP_GY, OR_DP_GZ,
+    OR_DP_DELTA, OR_DP_JAC, OR_DP_CURV, OR_DP_REG, OR_DP_REGIMG, OR_DP_POLYW, OR_DP_SINEW, OR_DP_POLYRES,
+    OR_DP_SINERES, OR_DP_RESULT, OR_DP_ROWS
+};
+
+/* Kinds: DoubleLayerKernel (HelmholtzKernel.c:613-761), new_HelmholtzKernelCombo
+ * (:173-610), new_HelmholtzKernel (:3-169). */
+enum { OR_DENSE_DOUBLE_LAYER = 0, OR_DENSE_COMBO = 1, OR_DENSE_SPHERE = 2 };
+
+/* Per-point arrays of one assembler, in the reference's lexicographic
+ * order.  pts (may be NULL) receives them when its point count equals
+ * n_alloc.  Returns the point count, or -(1 + position) of the first point
+ * whose interpolation cell falls outside the grid.  Grids are unused by
+ * the sphere kernel (may be NULL there). */
+int64_t or_dense_points(int kind, const or_params *p, const or_dense_opts *o, const double *d,
+                        const double *gx, const double *gy, const double *gz, const double *mcurv,
+                        const double *gcurv, int64_t n_alloc, double *pts);
+
+/* Dense n x n matrices (row-major) from the per-point arrays.  Double
+ * layer: K1 (re, im).  Combo and sphere kernel: K1 = the PolyWeight matrix
+ * (if o->poly), K2 = the SineWeight matrix (if o->sine); unused pointers
+ * may be NULL.  Returns the Combo's regcount (0 otherwise). */
+int64_t or_dense_matrix(int kind, const or_params *p, const or_dense_opts *o, int64_t n, const double *pts,
+                        double *k1re, double *k1im, double *k2re, double *k2im);
+
+/* PolyWeight / SineWeight of functions.c:793-866 (MOMENT_ORDER 1). */
+double or_poly_weight(double t, double tau);
+double or_sine_weight(double t, double tau);
+
 #ifdef __cplusplus
 }
 #endif

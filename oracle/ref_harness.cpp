@@ -46,6 +46,19 @@ int DoubleLayerKernel(int size, double epsilon, double ***level, double ***level
                       double *gradx, double *grady, double *gradz, double *delta, double *Jacobian, double *regfactor,
                       double *regfactorimg, double *result, double **Kernel, double **Kernelimg, double wavenum);
 
+int new_HelmholtzKernel(int size, double delta, double epsilon, double *zxlist, double *zylist, double *zzlist,
+                        double *zxstarlist, double *zystarlist, double *zzstarlist, double *dist, double *gradx,
+                        double *grady, double *gradz, double *curv, double *Jacobian, double *PolyW, double *SineW,
+                        double *PolyResult, double *SineResult, double **PolyKernelH, double **PolyKernelHimg,
+                        double **SineKernelH, double **SineKernelHimg);
+int new_HelmholtzKernelCombo(int size, double delta, double epsilon, double ***level, double ***leveldx,
+                             double ***leveldy, double ***leveldz, double ***levelmcurv, double ***levelgcurv,
+                             double *zxlist, double *zylist, double *zzlist, double *zxstarlist, double *zystarlist,
+                             double *zzstarlist, double *dist, double *gradx, double *grady, double *gradz,
+                             double *Jacobian, double *regfactor, double *regfactorimg, double *PolyW, double *SineW,
+                             double *PolyResult, double *SineResult, double **PolyKernelH, double **PolyKernelHimg,
+                             double **SineKernelH, double **SineKernelHimg, double wavenum, double eta);
+
 static double ***alloc_grid(int S)
 {
     double ***g = (double ***)malloc(S * sizeof(double **));
@@ -232,14 +245,14 @@ void ref_rows_matvec(int n, int r0, int r1, const double *pre, const double *pim
     }
 }
 
-/* DoubleLayerKernel (HelmholtzKernel.c:613-761): per-point arrays (16 x n,
- * in the order zx zy zz x* y* z* dist gx gy gz delta J reg regimg result
- * and an unused row) and the dense matrix, row-major. */
-int ref_double_layer(int n, double *pts, double *are, double *aim)
+/* DoubleLayerKernel (HelmholtzKernel.c:613-761): per-point arrays (20 x n,
+ * rows as below; curv and the weight rows stay untouched) and the dense
+ * matrix, row-major. */
+int ref_double_layer(int n, double epsilon, double *pts, double *are, double *aim)
 {
-    double eps = FACTOR * H;
-    double *a[16];
-    for (int r = 0; r < 16; r++) a[r] = pts + (size_t)r * n;
+    double eps = epsilon;
+    double *a[20];
+    for (int r = 0; r < 20; r++) a[r] = pts + (size_t)r * n;
     double **K = (double **)malloc(n * sizeof(double *));
     double **Ki = (double **)malloc(n * sizeof(double *));
     for (int i = 0; i < n; i++) {
@@ -247,10 +260,74 @@ int ref_double_layer(int n, double *pts, double *are, double *aim)
         Ki[i] = aim + (size_t)i * n;
     }
     int rc = DoubleLayerKernel(n, eps, DIST, DIST_DX, DIST_DY, DIST_DZ, MCURV, GCURV, a[0], a[1], a[2], a[3], a[4],
-                               a[5], a[6], a[7], a[8], a[9], a[10], a[11], a[12], a[13], a[14], K, Ki, WAVE);
+                               a[5], a[6], a[7], a[8], a[9], a[10], a[11], a[13], a[14], a[19], K, Ki, WAVE);
     free(K);
     free(Ki);
     return rc;
+}
+
+static double **rows_of(double *a, int n)
+{
+    double **r = (double **)malloc((size_t)(n > 0 ? n : 1) * sizeof(double *));
+    for (int i = 0; i < n; i++) r[i] = a + (size_t)i * n;
+    return r;
+}
+
+/* Row order of pts (20 x n) for the dense assemblers: zx zy zz xs ys zs
+ * dist gx gy gz delta jac curv reg regimg polyw sinew polyres sineres result. */
+
+/* new_HelmholtzKernelCombo (HelmholtzKernel.c:173-610) on the set-up grids:
+ * returns regcount.  k1 = the PolyWeight matrices, k2 = the SineWeight ones
+ * (only those of the build's POLY_TEST / SINE_TEST are written). */
+int ref_combo(int n, double delta0, double epsilon, double wavenum, double eta, double *pts, double *k1re,
+              double *k1im, double *k2re, double *k2im)
+{
+    double *a[20];
+    for (int r = 0; r < 20; r++) a[r] = pts + (size_t)r * n;
+    double **P = rows_of(k1re, n), **Pi = rows_of(k1im, n), **Sm = rows_of(k2re, n), **Si = rows_of(k2im, n);
+    int rc = new_HelmholtzKernelCombo(n, delta0, epsilon, DIST, DIST_DX, DIST_DY, DIST_DZ, MCURV, GCURV, a[0], a[1],
+                                      a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9], a[11], a[13], a[14], a[15], a[16],
+                                      a[17], a[18], P, Pi, Sm, Si, wavenum, eta);
+    free(P);
+    free(Pi);
+    free(Sm);
+    free(Si);
+    return rc;
+}
+
+/* new_HelmholtzKernel (HelmholtzKernel.c:3-169), the analytic sphere of frame.h. */
+int ref_sphere_kernel(int n, double delta0, double epsilon, double *pts, double *k1re, double *k1im, double *k2re,
+                      double *k2im)
+{
+    double *a[20];
+    for (int r = 0; r < 20; r++) a[r] = pts + (size_t)r * n;
+    double **P = rows_of(k1re, n), **Pi = rows_of(k1im, n), **Sm = rows_of(k2re, n), **Si = rows_of(k2im, n);
+    int rc = new_HelmholtzKernel(n, delta0, epsilon, a[0], a[1], a[2], a[3], a[4], a[5], a[6], a[7], a[8], a[9],
+                                 a[12], a[11], a[15], a[16], a[17], a[18], P, Pi, Sm, Si);
+    free(P);
+    free(Pi);
+    free(Sm);
+    free(Si);
+    return rc;
+}
+
+/* The reference build's switches of the dense assemblers. */
+void ref_dense_flags(int *out)
+{
+    out[0] = POLY_TEST;
+    out[1] = SINE_TEST;
+    out[2] = TRAD_ONESIDED;
+    out[3] = COMBO_ONESIDED;
+    out[4] = COMBO_INTERIOR;
+    out[5] = INTERIOR_MODE;
+}
+
+void ref_sphere(double *out)
+{
+    out[0] = radius;
+    out[1] = Cx;
+    out[2] = Cy;
+    out[3] = Cz;
 }
 
 /* CompBiCG (BICGSTAB.c:5-339) on a row-major dense matrix. */

@@ -7,7 +7,10 @@ the reference keeps its tube arrays in function statics.  Fixtures hold the
 input distance grid and the reference's outputs for it: WENO gradient and
 curvature grids, tube index list, per-point arrays, a sample of matrix
 entries, the dense products A p and A^H p for a seeded p, and the CompBiCG
-density for a point-source right-hand side solved to 1e-13.
+density for a point-source right-hand side solved to 1e-13.  The dense
+case holds the per-point arrays of the three dense assemblers of
+HelmholtzKernel.c, a sample of their matrix entries and their products with
+a seeded vector.
 
 Usage:  python oracle/build_ref.py && python tests/golden/make_golden.py
 """
@@ -36,6 +39,16 @@ CASES = {
     # the 3h tube inside the domain and away from the core circle at N=32)
     "ref_dirichlet_torus_n32": dict(variant="dirichlet", N=32, wave=4.0, shape="torus", R=0.5, r=0.25,
                                     rhs_kind=0),
+}
+
+
+# Dense assemblers of HelmholtzKernel.c on the reference's own configuration:
+# DoubleLayerKernel (tube |d| <= FACTOR h), new_HelmholtzKernelCombo on the
+# driver's default annulus [delta0, epsilon0] = [0.1 h, sqrt(h)] (eta -1,
+# large3Dexample2.c:37,61-63,298-305), new_HelmholtzKernel on frame.h's sphere.
+DENSE_CASES = {
+    "ref_neumann_dense_n16": dict(variant="neumann", N=16, wave=2.0, shape="sphere", radius=1.0,
+                                  center=(0.013, 0.021, 0.007), eta=-1.0),
 }
 
 
@@ -87,10 +100,71 @@ def run_case(name):
     return name, n
 
 
+def run_dense_case(name):
+    import oracle as O
+    case = DENSE_CASES[name]
+    ref = O.Reference(case["variant"])
+    N, k = case["N"], case["wave"]
+    d = distance(case, ref.int_l, ref.int_u)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    ref.setup(N, k, d)
+    fl = ref.dense_flags()
+    par = ref.params(N, k)
+    H = par.H
+    orc = O.Oracle()
+    grids = list(ref.grids())
+    rng = np.random.default_rng(4321)
+    out = dict(d=d)
+
+    def sample(K, n, tag):
+        pi = rng.integers(0, n, 1024)
+        pj = rng.integers(0, n, 1024)
+        pi[:32] = pj[:32]
+        v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        out[tag + "_pi"], out[tag + "_pj"] = pi, pj
+        out[tag + "_entries"] = K[pi, pj]
+        out[tag + "_v"] = v
+        out[tag + "_Kv"] = K @ v
+
+    def opts(delta0, eps, onesided, wavenum=k, eta=case["eta"]):
+        return O.DenseOpts(delta0, eps, wavenum, eta, fl["poly"], fl["sine"], onesided, fl["combo_interior"],
+                           fl["radius"], *fl["center"])
+
+    eps = ref.ref_eps()
+    od = opts(0.0, eps, fl["trad_onesided"])
+    n_dl = orc.L.or_dense_points(O.DENSE_DOUBLE_LAYER, O.C.byref(par), O.C.byref(od), O._d(d),
+                                 *[O._d(np.ascontiguousarray(g)) for g in grids], 0, None)
+    pts, K = ref.double_layer(n_dl, eps)
+    out["dl_pts"] = pts
+    sample(K, n_dl, "dl")
+    delta0, eps0 = 0.1 * H, np.sqrt(H)
+    oc = opts(delta0, eps0, fl["combo_onesided"])
+    n_c = orc.L.or_dense_points(O.DENSE_COMBO, O.C.byref(par), O.C.byref(oc), O._d(d),
+                                *[O._d(np.ascontiguousarray(g)) for g in grids], 0, None)
+    pts, KP, KS, regcount = ref.combo(n_c, delta0, eps0, k, case["eta"])
+    out["combo_pts"] = pts
+    sample(KS if fl["sine"] else KP, n_c, "combo")
+    n_s = orc.L.or_dense_points(O.DENSE_SPHERE, O.C.byref(par), O.C.byref(oc), None, None, None, None, None, None,
+                                0, None)
+    pts, KP, KS = ref.sphere_kernel(n_s, delta0, eps0)
+    out["sphere_pts"] = pts
+    sample(KS if fl["sine"] else KP, n_s, "sphere")
+    meta = dict(name=name, N=N, wave=k, int_l=ref.int_l, int_u=ref.int_u, factor=ref.factor,
+                tau_factor=ref.tau_factor, dirichlet=ref.dirichlet, interior=ref.interior, epsilon=eps,
+                delta0=delta0, epsilon0=eps0, eta=case["eta"], regcount=int(regcount), n_dl=int(n_dl),
+                n_combo=int(n_c), n_sphere=int(n_s), flags={k2: (v if not isinstance(v, tuple) else list(v))
+                                                           for k2, v in fl.items()})
+    meta["flags"]["radius"] = float(fl["radius"])
+    meta["flags"]["center"] = [float(c) for c in fl["center"]]
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **out)
+    return name, n_dl
+
+
 def main():
     # One process per case: the reference exits (status 0) on some inputs and
     # keeps per-process statics, so each case gets a fresh, time-limited child.
-    names = sys.argv[1:] or list(CASES)
+    names = sys.argv[1:] or list(CASES) + list(DENSE_CASES)
     for name in names:
         out = os.path.join(HERE, name + ".npz")
         if os.path.exists(out):
@@ -105,6 +179,9 @@ def main():
 
 if __name__ == "__main__":
     if len(sys.argv) == 3 and sys.argv[1] == "--one":
-        run_case(sys.argv[2])
+        if sys.argv[2] in DENSE_CASES:
+            run_dense_case(sys.argv[2])
+        else:
+            run_case(sys.argv[2])
     else:
         main()

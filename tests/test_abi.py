@@ -58,6 +58,9 @@ def test_reference_compat_symbols_exported(hz):
                                  check=True).stdout
             ref_syms |= {line.split()[-1] for line in out.splitlines() if line.strip()}
         for f in funcs:
+            if f.startswith("hz_"):  # extern "C" helpers of the drop-ins
+                assert f in syms, f
+                continue
             ours = [s for s in syms if re.fullmatch(r"_Z%d%s\w+" % (len(f), re.escape(f)), s)]
             assert ours, f
             if any(re.fullmatch(r"_Z%d%s\w+" % (len(f), re.escape(f)), s) for s in ref_syms):
