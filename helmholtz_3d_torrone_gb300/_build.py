@@ -24,8 +24,8 @@ UNITS = {
     "tube.cu": ["-fmad=false"],
     "dense.cu": ["-fmad=false"],
     "sweep_f64.cu": [],
-    "sweep_f32.cu": [],
-    "sweep_multi.cu": [],
+    "sweep_f32.cu": ["-ftz=true"],
+    "sweep_multi.cu": ["-ftz=true"],
     "krylov_multi.cu": [],
     "krylov.cu": [],
     "gmres.cu": [],
