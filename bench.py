@@ -39,11 +39,11 @@ if ROOT not in sys.path:
 METRIC = "256³ solve time & Gpair/s: FP32+FP64-refine vs plain FP64 GPU at 1e-6 rel err"
 FLOPS_PER_PAIR = 40  # reference pair formula, large3Dexample2.c:4471-4550
 # DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
-# 17.18 MB measured by ncu on the 128^3 torus (n = 145,272; see
+# 21.88 MB measured by ncu on the 128^3 torus (n = 145,272; see
 # profiles/sweep32_pair_torus_n128_full.md), scaled by n to n = 581,420.
 # The sweep reads every record once from DRAM and the tiles from L2, so
 # traffic grows in proportion to n.
-SWEEP32_TRAFFIC = 17.18e6 * 581420 / 145272
+SWEEP32_TRAFFIC = 21.88e6 * 581420 / 145272
 
 
 def parse():
@@ -69,6 +69,10 @@ def parse():
     ap.add_argument("--method", choices=["bicg", "gmres"], nargs="*", default=["bicg", "gmres"],
                     help="--solve: inner Krylov method(s) of the refined solves")
     ap.add_argument("--restart", type=int, default=40, help="--solve: GMRES restart length")
+    ap.add_argument("--shape", choices=["torus", "ellipsoid"], default="torus",
+                    help="--solve: torus (the step workload) or the ellipsoid (0.7,0.5,0.4) level set "
+                         "reinitialised on the device before the build")
+    ap.add_argument("--reinit-iters", type=int, default=60, help="--solve --shape ellipsoid: TVD-RK2 steps")
     ap.add_argument("--sweep-variant", type=int, default=-1,
                     help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
@@ -333,17 +337,34 @@ def run_solve(a, local):
     from helmholtz_3d_torrone_gb300 import geometry as G
 
     N, wave = a.N, a.wave
-    d = G.torus(N, R=0.6, r=0.25, int_l=-1.0, int_u=1.0)
+    H = 2.0 / N
+    t0 = time.perf_counter()
+    if a.shape == "ellipsoid":
+        # analytic non-distance level set of the ellipsoid, reinitialised on the
+        # device; its error against the exact ellipsoid distance is reported
+        phi = G.ellipsoid_levelset(N)
+        d = hz.reinitialize(phi, N, H, a.reinit_iters)
+        exact = G.ellipsoid(N)
+        band = np.abs(exact) <= 3 * H
+        reinit_err = float(np.max(np.abs(d - exact)[band]))
+        src = np.array([0.1, 0.05, 0.0])
+    else:
+        d = G.torus(N, R=0.6, r=0.25, int_l=-1.0, int_u=1.0)
+        src = np.array([0.6, 0.0, 0.0])
     p = hz.params(N, wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1)
     out = {"mode": "solve", "config": workload_desc(N, wave, 0), "runs": []}
     with hz.Operator(p) as op:
-        t0 = time.perf_counter()
         op.set_distance(d)
         n = op.build()
         out["build_s"] = time.perf_counter() - t0
         out["config"] = workload_desc(N, wave, n)
+        if a.shape == "ellipsoid":
+            out["config"]["workload"] = ("ellipsoid (0.7,0.5,0.4): level set 0.3(1-|x/a|) reinitialised by %d "
+                                         "TVD-RK2 steps on the device, %d^3 over [-1,1]^3, tube |phi|<=3h, k=%g, "
+                                         "Dirichlet point source at (0.1,0.05,0)" % (a.reinit_iters, N, wave))
+            out["config"]["reinit_max_err_in_band"] = reinit_err
         out["config"]["sweep_variant"] = op.autotune()[0]
-        b = op.rhs_point_source(np.array([0.6, 0.0, 0.0]), hz.RHS_POINT_DIRICHLET)
+        b = op.rhs_point_source(src, hz.RHS_POINT_DIRICHLET)
         sols = {}
         for meth in a.method:
             mid = hz.GMRES if meth == "gmres" else hz.BICG
@@ -360,9 +381,15 @@ def run_solve(a, local):
             x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=tol)
             info.update(precision="f64", tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
             out["runs"].append(info)
+            # off-surface field at 100 seeded receivers on the sphere r = 0.9
+            rx = G.random_sphere_points(100, 0.9, seed=7)
+            u64 = op.evaluate(rx, x64, hz.DOUBLE_LAYER)
             for (meth, t), x in sols.items():
                 out.setdefault("rel_err_vs_f64", {})["%s %g" % (meth, t)] = float(
                     np.max(np.abs(x - x64)) / np.max(np.abs(x64)))
+                u = op.evaluate(rx, x, hz.DOUBLE_LAYER)
+                out.setdefault("field_rel_err_vs_f64", {})["%s %g" % (meth, t)] = float(
+                    np.max(np.abs(u - u64)) / np.max(np.abs(u64)))
         elif a.fp64_iters > 0:
             x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=1e-300, maxit=a.fp64_iters,
                                  stagnation=0)

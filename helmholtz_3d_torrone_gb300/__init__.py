@@ -23,7 +23,7 @@ HZ_OK = 0
 HZ_HOST, HZ_DEVICE = 0, 1
 PREC_F64, PREC_F32, PREC_F32_REFINED = 0, 1, 2
 BICG, BICGSTAB, GMRES = 0, 1, 2
-SINGLE_LAYER, DOUBLE_LAYER = 0, 1
+SINGLE_LAYER, DOUBLE_LAYER, COMBO_LAYER = 0, 1, 2
 RHS_POINT_DIRICHLET, RHS_POINT_NEUMANN, RHS_MONOPOLE_NEUMANN, RHS_MONOPOLE_DIRICHLET = 0, 1, 2, 3
 NOALLOC_MAX_POINTS = 32768  # HZ_NOALLOC_MAX_POINTS
 
@@ -92,6 +92,15 @@ SIGNATURES = {
     "hz_set_stream": ([_vp, _vp], C.c_int),
     "hz_get_stream": ([_vp], _vp),
     "hz_set_distance": ([_vp, _vp, C.c_int], C.c_int),
+    "hz_set_combo": ([_vp, _vp], C.c_int),
+    "hz_batch_create": ([C.POINTER(_vp), C.c_int, C.POINTER(_vp)], C.c_int),
+    "hz_batch_destroy": ([_vp], None),
+    "hz_batch_autotune": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_double)], C.c_int),
+    "hz_batch_set_variant": ([_vp, C.c_int], C.c_int),
+    "hz_batch_matvec": ([_vp, C.c_int, C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.POINTER(_vp), C.c_int],
+                        C.c_int),
+    "hz_batch_solve": ([_vp, C.POINTER(SolveOpts)] + [C.POINTER(_vp)] * 4 + [C.c_int, C.POINTER(SolveInfo), _vp],
+                       C.c_int),
     "hz_build": ([_vp, C.POINTER(C.c_int64)], C.c_int),
     "hz_tube_size": ([_vp], C.c_int64),
     "hz_sweep_timing": ([_vp, C.c_int, _dp, C.POINTER(C.c_int64)], C.c_int),
@@ -229,6 +238,12 @@ class Operator:
 
     def set_stream(self, stream_handle):
         _check(load().hz_set_stream(self.h, stream_handle))
+
+    def set_combo(self, opts):
+        """Switch to the Combo formulation (before build); opts a DenseOpts
+        (see dense_opts(DENSE_COMBO, p)), None switches back."""
+        self._combo_opts = opts
+        _check(load().hz_set_combo(self.h, None if opts is None else C.byref(opts)))
 
     def set_distance(self, d, where=HZ_HOST):
         if where == HZ_HOST:
@@ -399,6 +414,63 @@ def dense_bicg(A, b, tol=1e-7, maxit=1000):
     _check(load().hz_dense_bicg(n, _ptr(are), _ptr(aim), _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), tol, maxit,
                                 HZ_HOST, C.byref(info)))
     return xr + 1j * xi, info.as_dict()
+
+
+# ------------------------------------------------------------------ batches
+class Batch:
+    """Independent built operators solved together (hz_batch_*): one
+    persistent FP32 launch per product over all of them."""
+
+    def __init__(self, ops):
+        self.ops = list(ops)
+        arr = (_vp * len(self.ops))(*[o.h for o in self.ops])
+        h = _vp()
+        _check(load().hz_batch_create(arr, len(self.ops), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if self.h:
+            load().hz_batch_destroy(self.h)
+            self.h = None
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()
+
+    def autotune(self):
+        cfg, ms = C.c_int(), C.c_double()
+        _check(load().hz_batch_autotune(self.h, C.byref(cfg), C.byref(ms)))
+        return cfg.value, ms.value
+
+    def set_variant(self, v):
+        _check(load().hz_batch_set_variant(self.h, v))
+
+    @staticmethod
+    def _ptrs(arrs):
+        return (_vp * len(arrs))(*[a.ctypes.data for a in arrs])
+
+    def matvec(self, vs, precision=PREC_F32):
+        pr = [_f64(v.real) for v in vs]
+        pi = [_f64(v.imag) for v in vs]
+        qr = [np.empty(o.n) for o in self.ops]
+        qi = [np.empty(o.n) for o in self.ops]
+        _check(load().hz_batch_matvec(self.h, precision, self._ptrs(pr), self._ptrs(pi), self._ptrs(qr),
+                                      self._ptrs(qi), HZ_HOST))
+        return [a + 1j * b for a, b in zip(qr, qi)]
+
+    def solve(self, bs, opts=None, **kw):
+        opts = opts if opts is not None else solve_opts(**kw)
+        br = [_f64(b.real) for b in bs]
+        bi = [_f64(b.imag) for b in bs]
+        xr = [np.empty(o.n) for o in self.ops]
+        xi = [np.empty(o.n) for o in self.ops]
+        info = SolveInfo()
+        res = np.empty(len(self.ops))
+        _check(load().hz_batch_solve(self.h, C.byref(opts), self._ptrs(br), self._ptrs(bi), self._ptrs(xr),
+                                     self._ptrs(xi), HZ_HOST, C.byref(info), _ptr(res)))
+        return [a + 1j * b for a, b in zip(xr, xi)], info.as_dict(), res
 
 
 # ------------------------------------------------------------ dense assemblers

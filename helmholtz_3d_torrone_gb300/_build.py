@@ -31,6 +31,8 @@ UNITS = {
     "gmres.cu": [],
     "evaluate.cu": [],
     "adjoint.cu": [],
+    "combo.cu": [],
+    "batch.cu": [],
     "capi.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],

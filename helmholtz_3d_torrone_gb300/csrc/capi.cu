@@ -128,6 +128,15 @@ struct MatrixFreeOp final : LinOp {
         const int slot = op->timer.slot();
         cudaEvent_t e0 = slot >= 0 ? op->timer.start[slot] : nullptr;
         cudaEvent_t e1 = slot >= 0 ? op->timer.stop[slot] : nullptr;
+        if (op->combo) {
+            if (precision != HZ_PREC_F64) {
+                set_error("the Combo formulation has FP64 products only");
+                return HZ_ERR_ARG;
+            }
+            return sweep_combo64(op->n, op->p.wave, op->combo_opts.wavenum, op->combo_opts.eta, op->tau,
+                                 op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->adist.as<double>(),
+                                 mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im, s, e0, e1);
+        }
         if (precision == HZ_PREC_F64)
             return sweep_f64(c, rec64(op), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im,
                              op->scratch.as<double2>(), s, e0, e1);
@@ -292,9 +301,70 @@ int need_built(hz_operator *op)
 
 }  // namespace
 
+// hz_build for the Combo formulation: annulus selection and per-point rows
+// of new_HelmholtzKernelCombo (dense.cu), packed into the operator's arrays.
+static int build_combo(hz_operator *op, int64_t *n_out)
+{
+    cudaStream_t s = op->stream;
+    int64_t n = 0;
+    HZ_TRY(dense_points_device(HZ_DENSE_COMBO, op->p, op->combo_opts, op->d.as<double>(), op->gx.as<double>(),
+                               op->gy.as<double>(), op->gz.as<double>(), op->mc.as<double>(), op->gc.as<double>(),
+                               op->idx, n, op->cpts, op->err.as<unsigned>(), s));
+    op->n = n;
+    const size_t nn = (size_t)(n > 0 ? n : 1);
+    HZ_TRY(op->xs.ensure(3 * nn * sizeof(double)));
+    HZ_TRY(op->nrm.ensure(3 * nn * sizeof(double)));
+    for (DevBuf *b : {&op->delta, &op->jac, &op->reg, &op->w, &op->dreg, &op->adist})
+        HZ_TRY(b->ensure(nn * sizeof(double)));
+    HZ_TRY(op->pos64.ensure(nn * sizeof(double4_32a)));
+    HZ_TRY(op->nrm64.ensure(nn * sizeof(double4_32a)));
+    HZ_TRY(combo_pack(n, op->cpts.as<double>(), op->combo_opts.sine, op->xs.as<double>(), op->nrm.as<double>(),
+                      op->delta.as<double>(), op->jac.as<double>(), op->reg.as<double>(), op->w.as<double>(),
+                      op->adist.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->dreg.ptr, 0, nn * sizeof(double), s));
+    HZ_TRY(check_device_error(op, "hz_build (Combo)"));
+    op->r32.npad = 0;  // no FP32 records: FP64 products only
+    HZ_TRY(op->scratch.ensure(nn * sizeof(double4_32a) + 256));
+    HZ_TRY(op->io.ensure(nn * sizeof(double) * 8));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    op->built = true;
+    hz_solver_state *st = solver_of(op);
+    if (st) {
+        st->outer.invalidate_graph();
+        st->inner.invalidate_graph();
+    }
+    if (n_out) *n_out = n;
+    return HZ_OK;
+}
+
+static int need_classic(hz_operator *op, const char *who)
+{
+    if (op && op->combo) {
+        set_error("%s is not available for the Combo formulation", who);
+        return HZ_ERR_STATE;
+    }
+    return HZ_OK;
+}
+
 extern "C" {
 
 const char *hz_last_error(void) { return g_err; }
+
+int hz_set_combo(hz_operator *op, const hz_dense_opts *o)
+{
+    if (!op) {
+        set_error("operator is NULL");
+        return HZ_ERR_ARG;
+    }
+    if (o && (!(o->epsilon > o->delta0) || !(o->delta0 >= 0) || (!o->poly && !o->sine) || (o->poly && o->sine))) {
+        set_error("hz_set_combo: need 0 <= delta0 < epsilon and exactly one of poly / sine");
+        return HZ_ERR_ARG;
+    }
+    op->combo = o ? 1 : 0;
+    if (o) op->combo_opts = *o;
+    op->built = false;
+    return HZ_OK;
+}
 
 int64_t hz_kernel_launches(void) { return g_launches.load(); }
 
@@ -427,6 +497,7 @@ int hz_build(hz_operator *op, int64_t *n_out)
     HZ_TRY(launch_grid_stencils(N, op->H, op->d.as<double>(), op->gx.as<double>(), op->gy.as<double>(),
                                 op->gz.as<double>(), op->mc.as<double>(), op->gc.as<double>(), op->p.weno_order, s));
     int64_t n = 0;
+    if (op->combo) return build_combo(op, n_out);
     HZ_TRY(tube_build(N, op->eps, op->d.as<double>(), op->idx, n, op->scratch, s));
     op->n = n;
     const size_t nn = (size_t)(n > 0 ? n : 1);
@@ -499,6 +570,7 @@ int64_t hz_tube_size(const hz_operator *op) { return op ? op->n : -1; }
 
 int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep)
 {
+    HZ_TRY(need_classic(op, "hz_autotune"));
     HZ_TRY(need_built(op));
     HZ_CHECK_CUDA(cudaSetDevice(op->device));
     cudaStream_t s = op->stream;
@@ -701,6 +773,7 @@ int hz_matvec_pair(hz_operator *op, int precision, const double *p_re, const dou
 int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re, const double *p_im,
                     double *q_re, double *q_im, int where)
 {
+    HZ_TRY(need_classic(op, "hz_matvec_multi"));
     HZ_TRY(need_built(op));
     HZ_TRY(where_ok(where));
     if (nrhs < 1 || precision < HZ_PREC_F64 || precision > HZ_PREC_F32_REFINED) {
@@ -737,6 +810,7 @@ int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re
 int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, const double *b_re, const double *b_im,
                    double *x_re, double *x_im, int where, hz_solve_info *info, double *resid)
 {
+    HZ_TRY(need_classic(op, "hz_solve_multi"));
     HZ_TRY(need_built(op));
     HZ_TRY(where_ok(where));
     hz_solve_opts o;
@@ -1001,6 +1075,10 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
     if (opts_in) o = *opts_in;
     else hz_solve_opts_default(&o);
     HZ_TRY(check_opts(o));
+    if (op->combo && o.precision != HZ_PREC_F64) {
+        set_error("hz_solve: the Combo formulation solves in FP64 only");
+        return HZ_ERR_ARG;
+    }
     HZ_CHECK_CUDA(cudaSetDevice(op->device));
     cudaStream_t s = op->stream;
     const int64_t n = op->n;
@@ -1037,6 +1115,7 @@ int hz_misfit_gradient(hz_operator *op, const hz_solve_opts *opts_in, const doub
                        int layer, int64_t m, const double *rx, const double *t_re, const double *t_im, double *J,
                        double *g_re, double *g_im, double *dJ_dk, double *dJ_dw, int where, hz_solve_info *info)
 {
+    HZ_TRY(need_classic(op, "hz_misfit_gradient"));
     HZ_TRY(need_built(op));
     HZ_TRY(where_ok(where));
     hz_solve_opts o;
@@ -1166,8 +1245,12 @@ int hz_eval(hz_operator *op, int layer, int64_t m, const double *rx, const doubl
 {
     HZ_TRY(need_built(op));
     HZ_TRY(where_ok(where));
-    if (layer != HZ_SINGLE_LAYER && layer != HZ_DOUBLE_LAYER) {
+    if (layer != HZ_SINGLE_LAYER && layer != HZ_DOUBLE_LAYER && layer != HZ_COMBO_LAYER) {
         set_error("unknown layer %d", layer);
+        return HZ_ERR_ARG;
+    }
+    if ((layer == HZ_COMBO_LAYER) != (op->combo != 0)) {
+        set_error("HZ_COMBO_LAYER goes with (and only with) the Combo formulation");
         return HZ_ERR_ARG;
     }
     if (m < 0) {
@@ -1192,8 +1275,12 @@ int hz_eval(hz_operator *op, int layer, int64_t m, const double *rx, const doubl
         dur = t + 3 * m + 2 * n;
         dui = dur + m;
     }
-    HZ_TRY(launch_eval(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), dsr, dsi, m, drx, op->p.wave,
-                       op->tau, op->p.interior, layer, dur, dui, s));
+    if (layer == HZ_COMBO_LAYER)
+        HZ_TRY(launch_eval_combo(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), dsr, dsi, m, drx,
+                                 op->p.wave, op->tau, op->combo_opts.eta, dur, dui, s));
+    else
+        HZ_TRY(launch_eval(op->n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), dsr, dsi, m, drx,
+                           op->p.wave, op->tau, op->p.interior, layer, dur, dui, s));
     if (where == HZ_HOST) {
         HZ_TRY(stage_out(u_re, dur, m, where, s));
         HZ_TRY(stage_out(u_im, dui, m, where, s));

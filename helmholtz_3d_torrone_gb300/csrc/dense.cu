@@ -484,6 +484,22 @@ int dense_assemble_device(int kind, const hz_params &p, const hz_dense_opts &o, 
     return HZ_OK;
 }
 
+int dense_points_device(int kind, const hz_params &p, const hz_dense_opts &o, const double *d, const double *gx,
+                        const double *gy, const double *gz, const double *mc, const double *gc, DevBuf &idx,
+                        int64_t &n, DevBuf &pts, unsigned *err, cudaStream_t s)
+{
+    const DenseArgs a = make_args(kind, p, o);
+    HZ_TRY(dense_select(a, d, idx, n, s));
+    const size_t rows = (size_t)HZ_DENSE_ROWS * (size_t)(n > 0 ? n : 1);
+    HZ_TRY(pts.ensure(rows * sizeof(double)));
+    HZ_CHECK_CUDA(cudaMemsetAsync(pts.ptr, 0, rows * sizeof(double), s));
+    if (n == 0) return HZ_OK;
+    dense_points_kernel<<<grid_for(n), 256, 0, s>>>(a, n, idx.as<int64_t>(), d, gx, gy, gz, mc, gc, pts.as<double>(),
+                                                     err);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
 int dense_count_device(int kind, const hz_params &p, const hz_dense_opts &o, const double *d, int64_t &n,
                        cudaStream_t s)
 {

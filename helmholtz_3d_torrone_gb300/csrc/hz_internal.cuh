@@ -147,6 +147,20 @@ int dense_assemble_device(int kind, const hz_params &p, const hz_dense_opts &o, 
                           long long *regcount, unsigned *err, cudaStream_t s);
 int dense_count_device(int kind, const hz_params &p, const hz_dense_opts &o, const double *d, int64_t &n,
                        cudaStream_t s);
+// selection (lexicographic node indices in idx) and per-point rows only
+int dense_points_device(int kind, const hz_params &p, const hz_dense_opts &o, const double *d, const double *gx,
+                        const double *gy, const double *gz, const double *mc, const double *gc, DevBuf &idx,
+                        int64_t &n, DevBuf &pts, unsigned *err, cudaStream_t s);
+// combo.cu: the Combo formulation as a matrix-free FP64 operator
+int combo_pack(int64_t n, const double *pts, int sine, double *xs, double *nrm, double *delta, double *jac,
+               double *reg, double *w, double *adist, double4_32a *pos64, double4_32a *nrm64, cudaStream_t s);
+int sweep_combo64(int64_t n, double wave, double wavenum, double eta, double tau, const double4_32a *pos,
+                  const double4_32a *nrm, const double *adist, int mode, const double *p_re, const double *p_im,
+                  const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re, double *qt_im,
+                  cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+int launch_eval_combo(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *s_re,
+                      const double *s_im, int64_t m, const double *rx, double wave, double tau, double eta,
+                      double *u_re, double *u_im, cudaStream_t s);
 // stencils.cu
 int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
                          double *mc, double *gc, int order, cudaStream_t s);
@@ -184,6 +198,21 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
 double sweep32_reg_scale(int interior);
 // number of compiled FP32 sweep variants (block shape x targets per thread)
 int sweep32_num_configs();
+// Batched FP32 products (sweep_f32.cu): Q[r] = A_r P[r] for R operators in
+// one persistent launch; P, Q are [R][stride] column arrays.
+struct Batch32Item {
+    SweepConst c;
+    Rec32 r;
+    const double4_32a *pos64;
+    float4 *dens;
+};
+size_t batch32_desc_bytes(int R);
+int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, int64_t &units, int64_t &blocks,
+                     cudaStream_t s);
+size_t batch32_partial_bytes();
+int sweep_f32_batch(int cfg, const void *desc_dev, int R, int64_t units, int64_t blocks, double4_32a *partial,
+                    size_t partial_bytes, const double *p_re, const double *p_im, double *q_re, double *q_im,
+                    int64_t stride, int64_t max_npad, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
 // bytes of stream-K scratch that every FP32 sweep variant fits in
 size_t sweep32_partial_bytes();
 
@@ -215,6 +244,10 @@ struct hz_operator {
     hz_solver_state *solver = nullptr;  // Krylov workspaces (capi.cu)
     hz::SweepTimer timer;
     int sweep_cfg = 0;  // FP32 sweep variant (hz_autotune)
+    // Combo formulation (hz_set_combo): annulus points, FP64 products only
+    int combo = 0;
+    hz_dense_opts combo_opts{};
+    hz::DevBuf adist, cpts;  // |d| per point; per-point rows of the selection
 };
 
 namespace hz {

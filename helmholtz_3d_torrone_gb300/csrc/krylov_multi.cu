@@ -222,11 +222,16 @@ int grid_x(int64_t n)
 
 KrylovMulti::~KrylovMulti()
 {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
     if (host) cudaFreeHost(host);
 }
 
 int KrylovMulti::reserve(int64_t n_, int R_)
 {
+    // a captured iteration refers to the old buffers and sizes
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    graph_key = 0;
     n = n_;
     R = R_;
     HZ_TRY(vecs.ensure((size_t)n * R * sizeof(double) * 2 * kVecs));
@@ -241,11 +246,46 @@ int KrylovMulti::reserve(int64_t n_, int R_)
 double *KrylovMulti::re(int v) { return vecs.as<double>() + (size_t)(2 * v) * n * R; }
 double *KrylovMulti::im(int v) { return vecs.as<double>() + (size_t)(2 * v + 1) * n * R; }
 
+int KrylovMulti::iteration(MultiOp &A, double tol, bool stagnation, int stall, cudaStream_t s)
+{
+    double *pp = partial.as<double>();
+    double *pp2 = pp + (size_t)R * kMB * 4;
+    MScal *sc = scal.as<MScal>();
+    const dim3 g(grid_x(n), R);
+    const int sb = (R + 127) / 128;
+    mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(RH), im(RH), pp);
+    HZ_CHECK_LAUNCH();
+    mbeta_kernel<<<sb, 128, 0, s>>>(R, pp, sc);
+    HZ_CHECK_LAUNCH();
+    mp_kernel<<<g, kMT, 0, s>>>(n, sc, re(RV), im(RV), re(P), im(P), re(V), im(V));
+    HZ_CHECK_LAUNCH();
+    HZ_TRY(A.apply(R, re(P), im(P), re(V), im(V), s));
+    mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(V), im(V), re(RH), im(RH), pp);
+    HZ_CHECK_LAUNCH();
+    malpha_kernel<<<sb, 128, 0, s>>>(R, pp, sc);
+    HZ_CHECK_LAUNCH();
+    ms_kernel<<<g, kMT, 0, s>>>(n, sc, re(RV), im(RV), re(V), im(V));
+    HZ_CHECK_LAUNCH();
+    HZ_TRY(A.apply(R, re(RV), im(RV), re(T), im(T), s));
+    mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(T), im(T), pp);
+    HZ_CHECK_LAUNCH();
+    mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(T), im(T), re(T), im(T), pp2);
+    HZ_CHECK_LAUNCH();
+    momega_kernel<<<sb, 128, 0, s>>>(R, pp, pp2, sc);
+    HZ_CHECK_LAUNCH();
+    mupdate_kernel<<<g, kMT, 0, s>>>(n, sc, re(X), im(X), re(RV), im(RV), re(P), im(P), re(T), im(T));
+    HZ_CHECK_LAUNCH();
+    mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(RV), im(RV), pp);
+    HZ_CHECK_LAUNCH();
+    merr_kernel<<<sb, 128, 0, s>>>(R, pp, sc, tol, stagnation ? 1 : 0, stall, host);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
 int KrylovMulti::solve(MultiOp &A, const double *b_re, const double *b_im, double tol, int maxit, bool stagnation,
                        cudaStream_t s, int &iters, std::vector<double> &resid, int stall)
 {
     double *pp = partial.as<double>();
-    double *pp2 = pp + (size_t)R * kMB * 4;
     MScal *sc = scal.as<MScal>();
     const dim3 g(grid_x(n), R);
     const int sb = (R + 127) / 128;
@@ -258,33 +298,44 @@ int KrylovMulti::solve(MultiOp &A, const double *b_re, const double *b_im, doubl
     HZ_CHECK_LAUNCH();
     iters = 0;
     resid.assign(R, 0.0);
+    const uint64_t key = A.key();
+    const int flags = (stagnation ? 1 : 0) | (stall << 1);
     for (int it = 1; it <= maxit; it++) {
-        mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(RH), im(RH), pp);
-        HZ_CHECK_LAUNCH();
-        mbeta_kernel<<<sb, 128, 0, s>>>(R, pp, sc);
-        HZ_CHECK_LAUNCH();
-        mp_kernel<<<g, kMT, 0, s>>>(n, sc, re(RV), im(RV), re(P), im(P), re(V), im(V));
-        HZ_CHECK_LAUNCH();
-        HZ_TRY(A.apply(R, re(P), im(P), re(V), im(V), s));
-        mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(V), im(V), re(RH), im(RH), pp);
-        HZ_CHECK_LAUNCH();
-        malpha_kernel<<<sb, 128, 0, s>>>(R, pp, sc);
-        HZ_CHECK_LAUNCH();
-        ms_kernel<<<g, kMT, 0, s>>>(n, sc, re(RV), im(RV), re(V), im(V));
-        HZ_CHECK_LAUNCH();
-        HZ_TRY(A.apply(R, re(RV), im(RV), re(T), im(T), s));
-        mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(T), im(T), pp);
-        HZ_CHECK_LAUNCH();
-        mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(T), im(T), re(T), im(T), pp2);
-        HZ_CHECK_LAUNCH();
-        momega_kernel<<<sb, 128, 0, s>>>(R, pp, pp2, sc);
-        HZ_CHECK_LAUNCH();
-        mupdate_kernel<<<g, kMT, 0, s>>>(n, sc, re(X), im(X), re(RV), im(RV), re(P), im(P), re(T), im(T));
-        HZ_CHECK_LAUNCH();
-        mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(RV), im(RV), pp);
-        HZ_CHECK_LAUNCH();
-        merr_kernel<<<sb, 128, 0, s>>>(R, pp, sc, tol, stagnation ? 1 : 0, stall, host);
-        HZ_CHECK_LAUNCH();
+        if (key) {
+            // one BiCGSTAB step per graph launch (captured on first use)
+            if (!graph_exec || graph_key != key || graph_stream != s || graph_tol != tol || graph_flags != flags) {
+                if (graph_exec) {
+                    cudaGraphExecDestroy(graph_exec);
+                    graph_exec = nullptr;
+                }
+                cudaGraph_t g = nullptr;
+                HZ_CHECK_CUDA(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+                const int rc = iteration(A, tol, stagnation, stall, s);
+                const cudaError_t ec = cudaStreamEndCapture(s, &g);
+                if (rc != HZ_OK) {
+                    if (g) cudaGraphDestroy(g);
+                    return rc;
+                }
+                if (ec != cudaSuccess) {
+                    set_error("multi right-hand-side solver: graph capture failed: %s", cudaGetErrorString(ec));
+                    return HZ_ERR_CUDA;
+                }
+                const cudaError_t ei = cudaGraphInstantiate(&graph_exec, g, 0);
+                cudaGraphDestroy(g);
+                if (ei != cudaSuccess) {
+                    graph_exec = nullptr;
+                    set_error("multi right-hand-side solver: graph instantiation failed: %s", cudaGetErrorString(ei));
+                    return HZ_ERR_CUDA;
+                }
+                graph_key = key;
+                graph_stream = s;
+                graph_tol = tol;
+                graph_flags = flags;
+            }
+            HZ_CHECK_CUDA(cudaGraphLaunch(graph_exec, s));
+        } else {
+            HZ_TRY(iteration(A, tol, stagnation, stall, s));
+        }
         HZ_CHECK_CUDA(cudaStreamSynchronize(s));
         iters = it;
         int active = 0;

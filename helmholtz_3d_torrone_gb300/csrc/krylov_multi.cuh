@@ -12,6 +12,10 @@ struct MultiOp {
     virtual ~MultiOp() = default;
     virtual int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im,
                       cudaStream_t s) = 0;
+    // nonzero: apply only enqueues kernels and copies on s (no allocation, no
+    // synchronisation), so a solver iteration around it can be captured in a
+    // CUDA graph; the value identifies the operator the graph was built for
+    virtual uint64_t key() const { return 0; }
 };
 
 class KrylovMulti {
@@ -26,10 +30,16 @@ class KrylovMulti {
     double *im(int v);
 
   private:
+    int iteration(MultiOp &A, double tol, bool stagnation, int stall, cudaStream_t s);
     int64_t n = 0;
     int R = 0;
     DevBuf vecs, partial, scal;
     double *host = nullptr;
+    cudaGraphExec_t graph_exec = nullptr;
+    uint64_t graph_key = 0;
+    cudaStream_t graph_stream = nullptr;
+    double graph_tol = 0.0;
+    int graph_flags = 0;
 };
 
 // sweep_multi.cu

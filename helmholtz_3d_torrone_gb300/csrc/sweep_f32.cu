@@ -33,6 +33,9 @@
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
 
+#include <cstring>
+#include <vector>
+
 namespace hz {
 namespace {
 
@@ -331,6 +334,276 @@ __global__ void __launch_bounds__(256) sweep32_fixup(Args32 a)
     }
 }
 
+// ------------------------------------------------------------ batches
+// One operator of a batch: its sweep arguments (records, densities,
+// constants) and its place in the batch's unit and block numbering.  The
+// product vectors are columns of [R][stride] arrays passed to the launch.
+struct BatchOp {
+    Args32 a;
+    int64_t unit0;   // first global (target block, source tile) unit
+    int64_t block0;  // first global target block
+    int64_t blocks, ntiles;
+    int dir;
+    double scale;    // sg / (4 pi), folded into the densities
+};
+
+struct BatchVec {
+    const double *p_re, *p_im;
+    double *q_re, *q_im;
+    int64_t stride;
+};
+
+// dens of every operator from its column of P (blockIdx.y = operator)
+__global__ void batch_prep_kernel(const BatchOp *__restrict__ ops, BatchVec v)
+{
+    const BatchOp &o = ops[blockIdx.y];
+    const double *pr = v.p_re + blockIdx.y * v.stride, *pi = v.p_im + blockIdx.y * v.stride;
+    float4 *dens = const_cast<float4 *>(o.a.dens);
+    for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < o.a.npad;
+         s += (int64_t)gridDim.x * blockDim.x) {
+        const int c = o.a.perm[s];
+        float4 d = make_float4(0.f, 0.f, 0.f, 0.f);
+        if (c >= 0) {
+            const double ws = o.a.tpos[s].w * o.scale;
+            d.x = (float)(ws * pr[c]);
+            d.y = (float)(ws * pi[c]);
+        }
+        dens[s] = d;
+    }
+}
+
+__device__ __forceinline__ int batch_op_of_unit(const BatchOp *ops, int nops, int64_t u, int from)
+{
+    int o = from;
+    while (o + 1 < nops && u >= ops[o + 1].unit0) o++;
+    return o;
+}
+
+__device__ __forceinline__ void batch_write(const Args32 &a, int64_t s, double ar, double ai, const double *p_re,
+                                            const double *p_im, double *q_re, double *q_im)
+{
+    const int c = a.perm[s];
+    if (c < 0) return;
+    if (!isfinite(ar) || !isfinite(ai)) atomicOr(a.err, DEV_ERR_NONFINITE);
+    q_re[c] = ar + 0.5 * p_re[c];
+    q_im[c] = ai + 0.5 * p_im[c];
+}
+
+// The tiles of one segment (one target block of one operator) for the
+// batched sweep: the same loop as sweep32_kernel with SWEEP_A.
+template <bool DIR, int NT, int TG>
+__device__ __forceinline__ bool batch_tiles(const Args32 &a, const BatchOp *ops, int nops, int o, int64_t &u,
+                                            int64_t seg_end, int64_t u_begin, int64_t u_end, int64_t blk,
+                                            int64_t slot0, const float3 (&th)[TG], const float3 (&tl)[TG],
+                                            const float3 (&tn)[TG], const float (&treg)[TG], float (&hAr)[TG],
+                                            float (&lAr)[TG], float (&hAi)[TG], float (&lAi)[TG],
+                                            float4 (*sp)[kTile32], float4 (*sn)[kTile32], float4 (*sd)[kTile32],
+                                            uint64_t *bar)
+{
+    constexpr int TS = kTile32;
+    constexpr int NTT = NT * TG / TS;
+    const int64_t ntiles = ops[o].ntiles, unit0 = ops[o].unit0;
+    const uint32_t *mrow = a.nearmask + (blk * NTT) * a.mwords;
+    for (; u < seg_end; u++) {
+        const int64_t it = u - u_begin;
+        const int buf = (int)(it & 1);
+        if (threadIdx.x == 0 && u + 1 < u_end) {
+            const int o2 = batch_op_of_unit(ops, nops, u + 1, o);
+            const int64_t base = ((u + 1 - ops[o2].unit0) % ops[o2].ntiles) * TS;
+            const uint32_t bytes = TS * sizeof(float4);
+            mbar_arrive_expect_tx(&bar[buf ^ 1], 3 * bytes);
+            bulk_g2s(&sp[buf ^ 1][0], ops[o2].a.pos + base, bytes, &bar[buf ^ 1]);
+            bulk_g2s(&sn[buf ^ 1][0], ops[o2].a.nrm + base, bytes, &bar[buf ^ 1]);
+            bulk_g2s(&sd[buf ^ 1][0], ops[o2].a.dens + base, bytes, &bar[buf ^ 1]);
+        }
+        const int64_t tile = u - unit0 - blk * ntiles;
+        uint32_t word = 0;
+#pragma unroll
+        for (int k = 0; k < NTT; k++) word |= __ldg(mrow + k * a.mwords + (tile >> 5));
+        const bool far = ((word >> (tile & 31)) & 1u) == 0;
+        const float4 oh = a.ohi[tile], ol = a.olo[tile];
+        float3 rel[TG];
+#pragma unroll
+        for (int g = 0; g < TG; g++)
+            rel[g] = make_float3((th[g].x - oh.x) + (tl[g].x - ol.x), (th[g].y - oh.y) + (tl[g].y - ol.y),
+                                 (th[g].z - oh.z) + (tl[g].z - ol.z));
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((it >> 1) & 1), kWaitLimit);
+        if (__syncthreads_or(!ok)) {
+            if (threadIdx.x == 0) {
+                atomicOr(a.err, DEV_ERR_WAIT);
+                if (u + 1 < u_end) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimit);
+            }
+            return false;
+        }
+        float fAr[TG], fAi[TG], fHr[TG], fHi[TG];
+#pragma unroll
+        for (int g = 0; g < TG; g++) fAr[g] = fAi[g] = fHr[g] = fHi[g] = 0.f;
+        const int64_t base = tile * TS;
+        if (far) {
+#pragma unroll 2
+            for (int j = 0; j < TS; j++)
+                pair_block<SWEEP_A, DIR, NT, TG, false>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
+                                                        base + j, fAr, fAi, fHr, fHi);
+        } else {
+#pragma unroll 2
+            for (int j = 0; j < TS; j++)
+                pair_block<SWEEP_A, DIR, NT, TG, true>(a, sp[buf][j], sn[buf][j], sd[buf][j], rel, tn, treg, slot0,
+                                                       base + j, fAr, fAi, fHr, fHi);
+        }
+#pragma unroll
+        for (int g = 0; g < TG; g++) {
+            two_sum_acc(hAr[g], lAr[g], fAr[g]);
+            two_sum_acc(hAi[g], lAi[g], fAi[g]);
+        }
+        __syncthreads();
+    }
+    return true;
+}
+
+// Q[r] = A_r P[r] for every operator r of a batch in one persistent launch:
+// the stream-K partition of sweep32_kernel over the concatenated
+// (operator, target block, source tile) units, so operators of different
+// sizes share the GPU without a tail per operator.
+template <int NT, int TG, int MINB>
+__global__ void __launch_bounds__(NT, MINB) sweep32_batch_kernel(const BatchOp *__restrict__ ops, int nops,
+                                                                 int64_t units, int64_t nctas,
+                                                                 double4_32a *partial, BatchVec v)
+{
+    constexpr int TS = kTile32;
+    constexpr int SLOTS = NT * TG;
+    __shared__ alignas(128) float4 sp[2][TS];
+    __shared__ alignas(128) float4 sn[2][TS];
+    __shared__ alignas(128) float4 sd[2][TS];
+    __shared__ alignas(8) uint64_t bar[2];
+    const int64_t u_begin = (int64_t)blockIdx.x * units / nctas;
+    const int64_t u_end = ((int64_t)blockIdx.x + 1) * units / nctas;
+    if (threadIdx.x == 0) {
+        mbar_init(&bar[0], 1);
+        mbar_init(&bar[1], 1);
+        fence_barrier_init();
+    }
+    __syncthreads();
+    if (u_begin >= u_end) return;
+    int o = batch_op_of_unit(ops, nops, u_begin, 0);
+    if (threadIdx.x == 0) {
+        const int64_t base = ((u_begin - ops[o].unit0) % ops[o].ntiles) * TS;
+        const uint32_t bytes = TS * sizeof(float4);
+        mbar_arrive_expect_tx(&bar[0], 3 * bytes);
+        bulk_g2s(&sp[0][0], ops[o].a.pos + base, bytes, &bar[0]);
+        bulk_g2s(&sn[0][0], ops[o].a.nrm + base, bytes, &bar[0]);
+        bulk_g2s(&sd[0][0], ops[o].a.dens + base, bytes, &bar[0]);
+    }
+    int seg = 0;
+    for (int64_t u = u_begin; u < u_end;) {
+        o = batch_op_of_unit(ops, nops, u, o);
+        const Args32 a = ops[o].a;
+        const int64_t ntiles = ops[o].ntiles, unit0 = ops[o].unit0;
+        const int64_t blk = (u - unit0) / ntiles;
+        const int64_t blk_end = unit0 + (blk + 1) * ntiles;
+        const int64_t seg_end = (u_end < blk_end) ? u_end : blk_end;
+        const bool whole = (u == unit0 + blk * ntiles) && (seg_end == blk_end);
+        const int64_t slot0 = blk * SLOTS + threadIdx.x;
+        float3 th[TG], tl[TG], tn[TG];
+        float treg[TG];
+        float hAr[TG], lAr[TG], hAi[TG], lAi[TG];
+#pragma unroll
+        for (int g = 0; g < TG; g++) {
+            const int64_t s = slot0 + (int64_t)g * NT;
+            const float4 h = a.thi[s], l = a.tlo[s], nn = a.nrm[s];
+            th[g] = make_float3(h.x, h.y, h.z);
+            tl[g] = make_float3(l.x, l.y, l.z);
+            tn[g] = make_float3(nn.x, nn.y, nn.z);
+            treg[g] = a.pos[s].w;
+            hAr[g] = lAr[g] = hAi[g] = lAi[g] = 0.f;
+        }
+        const bool ok = ops[o].dir
+                            ? batch_tiles<true, NT, TG>(a, ops, nops, o, u, seg_end, u_begin, u_end, blk, slot0, th,
+                                                        tl, tn, treg, hAr, lAr, hAi, lAi, sp, sn, sd, bar)
+                            : batch_tiles<false, NT, TG>(a, ops, nops, o, u, seg_end, u_begin, u_end, blk, slot0, th,
+                                                         tl, tn, treg, hAr, lAr, hAi, lAi, sp, sn, sd, bar);
+        if (!ok) return;
+        const double *pr = v.p_re + o * v.stride, *pi = v.p_im + o * v.stride;
+        double *qr = v.q_re + o * v.stride, *qi = v.q_im + o * v.stride;
+#pragma unroll
+        for (int g = 0; g < TG; g++) {
+            const double ar = (double)hAr[g] + (double)lAr[g], ai = (double)hAi[g] + (double)lAi[g];
+            if (whole)
+                batch_write(a, slot0 + (int64_t)g * NT, ar, ai, pr, pi, qr, qi);
+            else
+                partial[((int64_t)blockIdx.x * 2 + seg) * SLOTS + threadIdx.x + g * NT] =
+                    make_double4_32a(ar, ai, 0.0, 0.0);
+        }
+        seg = 1;
+    }
+}
+
+// The batch's split blocks, summed in CTA order (one CTA per global block).
+template <int SLOTS>
+__global__ void __launch_bounds__(256) sweep32_batch_fixup(const BatchOp *__restrict__ ops, int nops, int64_t units,
+                                                           int64_t nctas, const double4_32a *partial, BatchVec v)
+{
+    const int64_t gb = blockIdx.x;
+    int o = 0;
+    while (o + 1 < nops && gb >= ops[o + 1].block0) o++;
+    const int64_t blk = gb - ops[o].block0, ntiles = ops[o].ntiles;
+    const int64_t u0 = ops[o].unit0 + blk * ntiles;
+    const int64_t c_lo = cta_of_unit(u0, units, nctas), c_hi = cta_of_unit(u0 + ntiles - 1, units, nctas);
+    if (c_lo == c_hi) return;
+    const Args32 &a = ops[o].a;
+    for (int k = threadIdx.x; k < SLOTS; k += blockDim.x) {
+        double ar = 0.0, ai = 0.0;
+        for (int64_t c = c_lo; c <= c_hi; c++) {
+            const int64_t ub = c * units / nctas;
+            const int oc = batch_op_of_unit(ops, nops, ub, 0);
+            const int64_t first = ops[oc].block0 + (ub - ops[oc].unit0) / ops[oc].ntiles;
+            const int sg = (first == gb) ? 0 : 1;
+            const double4_32a q = partial[(c * 2 + sg) * SLOTS + k];
+            ar += q.x;
+            ai += q.y;
+        }
+        batch_write(a, blk * SLOTS + k, ar, ai, v.p_re + o * v.stride, v.p_im + o * v.stride, v.q_re + o * v.stride,
+                    v.q_im + o * v.stride);
+    }
+}
+
+template <int NT, int TG, int MINB>
+int64_t batch_resident_ctas()
+{
+    static int64_t cached = 0;
+    if (cached == 0) {
+        int dev = 0, sms = 152, per = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, sweep32_batch_kernel<NT, TG, MINB>, NT, 0) !=
+                cudaSuccess ||
+            per < 1) {
+            cudaGetLastError();
+            per = MINB;
+        }
+        cached = (int64_t)per * sms;
+    }
+    return cached;
+}
+
+template <int NT, int TG, int MINB>
+int launch_batch(const BatchOp *ops_dev, int nops, int64_t units, int64_t blocks, double4_32a *partial,
+                 size_t partial_bytes, const BatchVec &v, cudaStream_t s)
+{
+    constexpr int SLOTS = NT * TG;
+    int64_t p = batch_resident_ctas<NT, TG, MINB>();
+    if (p > units) p = units;
+    if ((size_t)p * 2 * SLOTS * sizeof(double4_32a) > partial_bytes) p = partial_bytes / (2 * SLOTS * sizeof(double4_32a));
+    if (p < 1) {
+        set_error("batched FP32 sweep: partial buffer too small");
+        return HZ_ERR_STATE;
+    }
+    sweep32_batch_kernel<NT, TG, MINB><<<(unsigned)p, NT, 0, s>>>(ops_dev, nops, units, p, partial, v);
+    HZ_CHECK_LAUNCH();
+    sweep32_batch_fixup<SLOTS><<<(unsigned)blocks, 256, 0, s>>>(ops_dev, nops, units, p, partial, v);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
 // Resident CTAs of one sweep instantiation on this device (cached).
 template <int MODE, bool DIR, int NT, int TG, int MINB>
 int64_t resident_ctas()
@@ -442,6 +715,99 @@ size_t sweep32_partial_bytes()
     size_t m = 0;
     for (size_t x : v) m = x > m ? x : m;
     return m;
+}
+
+// ---------------------------------------------------------------- batches
+size_t batch32_desc_bytes(int R) { return (size_t)R * sizeof(BatchOp); }
+
+int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, int64_t &units, int64_t &blocks,
+                     cudaStream_t s)
+{
+    static const int kSlots[kShapes] = {512, 256, 256, 256};  // NT * TG of shapes 0..3 (launch_cfg)
+    const int slots = kSlots[cfg % kShapes];
+    std::vector<BatchOp> h(R);
+    units = 0;
+    blocks = 0;
+    for (int r = 0; r < R; r++) {
+        const Batch32Item &it = items[r];
+        BatchOp &b = h[r];
+        memset(&b, 0, sizeof(b));
+        Args32 &a = b.a;
+        a.n = it.c.n;
+        a.npad = it.r.npad;
+        a.mwords = it.r.mwords;
+        a.wave = (float)it.c.wave;
+        split_wave(it.c.wave, a.kh, a.kl);
+        a.tau = it.c.tau;
+        a.tau2 = (float)(it.c.tau * it.c.tau);
+        a.guard_lo = (float)(it.c.tau * it.c.tau * (1.0 - 1e-4));
+        a.guard_hi = (float)(it.c.tau * it.c.tau * (1.0 + 1e-4));
+        a.pos = it.r.pos;
+        a.nrm = it.r.nrm;
+        a.dens = it.dens;
+        a.thi = it.r.thi;
+        a.tlo = it.r.tlo;
+        a.ohi = it.r.ohi;
+        a.olo = it.r.olo;
+        a.nearmask = it.r.nearmask;
+        a.tpos = it.r.tpos;
+        a.perm = it.r.perm;
+        a.pos64 = it.pos64;
+        a.err = it.c.err;
+        if (it.r.npad % slots != 0) {
+            set_error("batched FP32 sweep: operator %d has %lld slots, not a multiple of %d", r,
+                      (long long)it.r.npad, slots);
+            return HZ_ERR_STATE;
+        }
+        b.ntiles = it.r.npad / kTile32;
+        b.blocks = it.r.npad / slots;
+        b.unit0 = units;
+        b.block0 = blocks;
+        b.dir = it.c.dirichlet != 0;
+        b.scale = ((it.c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi);
+        units += b.blocks * b.ntiles;
+        blocks += b.blocks;
+    }
+    HZ_CHECK_CUDA(cudaMemcpyAsync(desc_dev, h.data(), R * sizeof(BatchOp), cudaMemcpyHostToDevice, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    return HZ_OK;
+}
+
+size_t batch32_partial_bytes()
+{
+    const size_t v[kShapes] = {
+        (size_t)batch_resident_ctas<256, 2, 2>() * 2 * 512 * sizeof(double4_32a),
+        (size_t)batch_resident_ctas<128, 2, 4>() * 2 * 256 * sizeof(double4_32a),
+        (size_t)batch_resident_ctas<256, 1, 3>() * 2 * 256 * sizeof(double4_32a),
+        (size_t)batch_resident_ctas<128, 2, 6>() * 2 * 256 * sizeof(double4_32a)};
+    size_t m = 0;
+    for (size_t x : v) m = x > m ? x : m;
+    return m;
+}
+
+int sweep_f32_batch(int cfg, const void *desc_dev, int R, int64_t units, int64_t blocks, double4_32a *partial,
+                    size_t partial_bytes, const double *p_re, const double *p_im, double *q_re, double *q_im,
+                    int64_t stride, int64_t max_npad, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
+{
+    if (R <= 0 || units <= 0) return HZ_OK;
+    const BatchOp *ops = static_cast<const BatchOp *>(desc_dev);
+    BatchVec v{p_re, p_im, q_re, q_im, stride};
+    // padded tails of the columns stay zero
+    HZ_CHECK_CUDA(cudaMemsetAsync(q_re, 0, (size_t)R * stride * sizeof(double), s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(q_im, 0, (size_t)R * stride * sizeof(double), s));
+    long long bx = (max_npad + 255) / 256;
+    if (bx > 256) bx = 256;
+    batch_prep_kernel<<<dim3((unsigned)bx, (unsigned)R), 256, 0, s>>>(ops, v);
+    HZ_CHECK_LAUNCH();
+    if (ev0) HZ_CHECK_CUDA(record_timing_event(ev0, s));
+    switch (cfg % kShapes) {
+    case 1: HZ_TRY((launch_batch<128, 2, 4>(ops, R, units, blocks, partial, partial_bytes, v, s))); break;
+    case 2: HZ_TRY((launch_batch<256, 1, 3>(ops, R, units, blocks, partial, partial_bytes, v, s))); break;
+    case 3: HZ_TRY((launch_batch<128, 2, 6>(ops, R, units, blocks, partial, partial_bytes, v, s))); break;
+    default: HZ_TRY((launch_batch<256, 2, 2>(ops, R, units, blocks, partial, partial_bytes, v, s))); break;
+    }
+    if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
+    return HZ_OK;
 }
 
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode, const double *p_re,

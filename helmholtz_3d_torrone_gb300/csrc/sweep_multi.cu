@@ -5,7 +5,9 @@
 // computed once and multiplied into RB densities, so the per-RHS cost falls
 // from a full pair evaluation to four fused multiply-adds.  Both precisions
 // follow the single-vector sweeps (sweep_f32.cu, sweep_f64.cu) for the
-// kernel arithmetic, tiling, TMA staging and the near-field rules; the
+// kernel arithmetic, tiling, TMA staging and the near-field rules (the FP32
+// pass uses the same near-tile mask, head/tail target offsets and TwoSum
+// cross-tile sums, with no FP64 instruction in its tile loop); the
 // densities of a tile are staged as RB/2 rows of two complex values each.
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
@@ -19,18 +21,30 @@ constexpr int kRB = 8;  // right-hand sides per kernel pass
 
 // ------------------------------------------------------------------ FP32
 struct ArgsM32 {
-    int64_t n, npad;
+    int64_t n, npad, mwords;
     int nr;  // right-hand sides in this pass (<= kRB)
     float wave, kh, kl, tau2, guard_lo, guard_hi;
-    double tau, tau_far;
+    double tau;
     const float4 *pos, *nrm;
     const float4 *dens;  // [kRB/2][npad]: (p'_{2q} re, im, p'_{2q+1} re, im)
-    const double4_32a *origin, *tpos, *pos64;
+    const float4 *thi, *tlo, *ohi, *olo;
+    const uint32_t *nearmask;
+    const double4_32a *tpos, *pos64;
     const int *perm;
     const double *p_re, *p_im;  // [nr][n] (diagonal term)
     double *q_re, *q_im;        // [nr][n]
     unsigned *err;
 };
+
+// hi + lo += f without rounding loss (TwoSum, FP32 only)
+__device__ __forceinline__ void two_sum_m(float &hi, float &lo, float f)
+{
+    const float s = hi + f;
+    const float bp = s - hi;
+    const float e = (hi - (s - bp)) + (f - bp);
+    hi = s;
+    lo += e;
+}
 
 __global__ void prepm32_kernel(int64_t n, int64_t npad, int nr, const int *__restrict__ perm,
                                const double4_32a *__restrict__ tpos, const double *__restrict__ p_re,
@@ -60,7 +74,7 @@ __global__ void prepm32_kernel(int64_t n, int64_t npad, int nr, const int *__res
 
 template <bool DIR, bool NEAR>
 __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, const float4 s_n, const float3 rel,
-                                        const float3 tn, float treg, const double4_32a &tp, int64_t src_slot,
+                                        const float3 tn, float treg, int64_t tslot, int64_t src_slot,
                                         const float4 *sd, int j, float (&acc)[2 * kRB])
 {
     const float dx = rel.x - s_p.x, dy = rel.y - s_p.y, dz = rel.z - s_p.z;
@@ -72,6 +86,7 @@ __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, cons
             const int c = a.perm[src_slot];
             if (c >= 0) {
                 const double4_32a q = a.pos64[c];
+                const double4_32a tp = a.tpos[tslot];
                 const double x1 = tp.x - q.x, x2 = tp.y - q.y, x3 = tp.z - q.z;
                 const double rr2 = x1 * x1 + x2 * x2 + x3 * x3;
                 near = !(sqrt(rr2) > a.tau);
@@ -80,7 +95,7 @@ __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, cons
     }
     const float rinv = rsqrtf(r2);
     const float rho = r2 * rinv;
-    const float nn = rintf(rho * a.kh);
+    const float nn = fmaf(rho, a.kh, 12582912.f) - 12582912.f;  // nearest integer, |rho kh| < 2^22
     float f = fmaf(rho, a.kh, -nn);
     f = fmaf(rho, a.kl, f);
     float S, C;
@@ -115,14 +130,16 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
     __shared__ alignas(8) uint64_t bar[2];
     float4 *sp[2] = {smem32, smem32 + (2 + kRB / 2) * TS};
     const int64_t slot = (int64_t)blockIdx.x * kNT32m + threadIdx.x;
-    const double4_32a tp = a.tpos[slot];
+    const float4 th = a.thi[slot], tl = a.tlo[slot];
     const float4 nn4 = a.nrm[slot];
     const float3 tn = make_float3(nn4.x, nn4.y, nn4.z);
     const float treg = a.pos[slot].w;
-    const double4_32a tsph = a.origin[slot / TS];
-    double accd[2 * kRB];
+    // near-tile mask row of this block's target tile (kNT32m == kTile32)
+    const uint32_t *mrow = a.nearmask + (slot / TS) * a.mwords;
+    // cross-tile sums: FP32 head + tail (TwoSum)
+    float acch[2 * kRB], accl[2 * kRB];
 #pragma unroll
-    for (int i = 0; i < 2 * kRB; i++) accd[i] = 0.0;
+    for (int i = 0; i < 2 * kRB; i++) acch[i] = accl[i] = 0.f;
     const int64_t ntiles = a.npad / TS;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -143,10 +160,10 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
     for (int64_t tile = 0; tile < ntiles; tile++) {
         const int buf = (int)(tile & 1);
         if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
-        const double4_32a o = a.origin[tile];
-        const double ex = o.x - tsph.x, ey = o.y - tsph.y, ez = o.z - tsph.z;
-        const bool far = sqrt(ex * ex + ey * ey + ez * ez) - o.w - tsph.w > a.tau_far;
-        const float3 rel = make_float3((float)(tp.x - o.x), (float)(tp.y - o.y), (float)(tp.z - o.z));
+        const bool far = ((__ldg(mrow + (tile >> 5)) >> (tile & 31)) & 1u) == 0;
+        const float4 oh = a.ohi[tile], ol = a.olo[tile];
+        const float3 rel = make_float3((th.x - oh.x) + (tl.x - ol.x), (th.y - oh.y) + (tl.y - ol.y),
+                                       (th.z - oh.z) + (tl.z - ol.z));
         const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
@@ -161,12 +178,12 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
         for (int i = 0; i < 2 * kRB; i++) acc[i] = 0.f;
         const int64_t base = tile * TS;
         if (far) {
-            for (int j = 0; j < TS; j++) pairm32<DIR, false>(a, P[j], Nn[j], rel, tn, treg, tp, base + j, D, j, acc);
+            for (int j = 0; j < TS; j++) pairm32<DIR, false>(a, P[j], Nn[j], rel, tn, treg, slot, base + j, D, j, acc);
         } else {
-            for (int j = 0; j < TS; j++) pairm32<DIR, true>(a, P[j], Nn[j], rel, tn, treg, tp, base + j, D, j, acc);
+            for (int j = 0; j < TS; j++) pairm32<DIR, true>(a, P[j], Nn[j], rel, tn, treg, slot, base + j, D, j, acc);
         }
 #pragma unroll
-        for (int i = 0; i < 2 * kRB; i++) accd[i] += acc[i];
+        for (int i = 0; i < 2 * kRB; i++) two_sum_m(acch[i], accl[i], acc[i]);
         __syncthreads();
     }
     const int c = a.perm[slot];
@@ -174,7 +191,8 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
 #pragma unroll
     for (int r = 0; r < kRB; r++) {
         if (r >= a.nr) break;
-        const double vr = accd[2 * r], vi = accd[2 * r + 1];
+        const double vr = (double)acch[2 * r] + (double)accl[2 * r];
+        const double vi = (double)acch[2 * r + 1] + (double)accl[2 * r + 1];
         if (!isfinite(vr) || !isfinite(vi)) atomicOr(a.err, DEV_ERR_NONFINITE);
         a.q_re[(int64_t)r * a.n + c] = vr + 0.5 * a.p_re[(int64_t)r * a.n + c];
         a.q_im[(int64_t)r * a.n + c] = vi + 0.5 * a.p_im[(int64_t)r * a.n + c];
@@ -414,14 +432,18 @@ int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int pre
             a.wave = (float)c.wave;
             split_wave(c.wave, a.kh, a.kl);
             a.tau = c.tau;
-            a.tau_far = c.tau * (1.0 + 1e-3);
+            a.mwords = r32.mwords;
             a.tau2 = (float)(c.tau * c.tau);
             a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
             a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
             a.pos = r32.pos;
             a.nrm = r32.nrm;
             a.dens = dens;
-            a.origin = r32.origin;
+            a.thi = r32.thi;
+            a.tlo = r32.tlo;
+            a.ohi = r32.ohi;
+            a.olo = r32.olo;
+            a.nearmask = r32.nearmask;
             a.tpos = r32.tpos;
             a.pos64 = r64.pos;
             a.perm = r32.perm;

@@ -65,7 +65,10 @@ def ellipsoid(N, axes=(0.7, 0.5, 0.4), int_l=-1.0, int_u=1.0, iters=60):
         others = [i for i in range(3) if i != im]
         xd = np.zeros((int(deg.sum()), 3))
         for i in others:
-            xd[:, i] = a[i] ** 2 * y[deg, i] / (a[i] ** 2 - a[im] ** 2)
+            gap = a[i] ** 2 - a[im] ** 2
+            # an axis as short as the shortest one: the closest point keeps
+            # no component along it (only the centre plane is degenerate)
+            xd[:, i] = a[i] ** 2 * y[deg, i] / gap if gap > 0 else 0.0
         rest = 1.0 - sum((xd[:, i] / a[i]) ** 2 for i in others)
         xd[:, im] = a[im] * np.sqrt(np.maximum(rest, 0.0))
         x[deg] = xd

@@ -68,6 +68,8 @@ extern "C" {
 /* Evaluation layers. */
 #define HZ_SINGLE_LAYER 0 /* NeumannTest, large3Dexample2.c:1810-1824 */
 #define HZ_DOUBLE_LAYER 1 /* the Dirichlet matrix's kernel off the surface */
+#define HZ_COMBO_LAYER 2  /* Combo formulation: dG/dn_y - i eta G, Combo_NeumannTest
+                             (large3Dexample2.c:1907-2059); needs hz_set_combo */
 
 /* Boundary data kinds for hz_rhs_point_source. */
 #define HZ_RHS_POINT_DIRICHLET 0 /* g = e^{ik|x-s|}/(4 pi |x-s|)                        */
@@ -306,6 +308,44 @@ HZ_API int hz_dense_assemble(int kind, const hz_params *p, const hz_dense_opts *
                              const double *gx, const double *gy, const double *gz, const double *mc,
                              const double *gc, int64_t n, double *pts, double *k1_re, double *k1_im,
                              double *k2_re, double *k2_im, int64_t *regcount, int where);
+
+/* ---- Batches of operators ------------------------------------------------
+ * Independent surfaces (each its own built operator: grid, tube, k may
+ * differ) solved together: every FP32 product of the batch is ONE
+ * persistent launch whose CTAs share the (operator, target block, source
+ * tile) work of all operators, so small and large tubes fill the GPU
+ * together; the lockstep BiCGSTAB iteration around it runs as one CUDA
+ * graph.  Vectors are passed per operator: arrays of `count` pointers, the
+ * r-th of length hz_tube_size(ops[r]).  The operators must be built, use
+ * the classic formulation and live on the same device; the batch keeps
+ * pointers to them (destroy the batch first). */
+typedef struct hz_batch hz_batch;
+HZ_API int hz_batch_create(hz_operator *const *ops, int count, hz_batch **out);
+HZ_API void hz_batch_destroy(hz_batch *b);
+/* Time the FP32 batch sweep shapes and keep the fastest (variant, ms). */
+HZ_API int hz_batch_autotune(hz_batch *b, int *chosen, double *ms_per_sweep);
+/* Use batch sweep shape v (0..3) instead of the autotuner's choice. */
+HZ_API int hz_batch_set_variant(hz_batch *b, int v);
+/* q_r = A_r p_r for every operator: HZ_PREC_F32 (one persistent launch) or
+ * HZ_PREC_F64 (one FP64 sweep per operator). */
+HZ_API int hz_batch_matvec(hz_batch *b, int precision, const double *const *p_re, const double *const *p_im,
+                           double *const *q_re, double *const *q_im, int where);
+/* Solve A_r x_r = b_r for all r with lockstep BiCGSTAB (opts->method is
+ * ignored); HZ_PREC_F32_REFINED refines every system with its FP64
+ * residual.  resid (may be NULL): count final relative residuals. */
+HZ_API int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts, const double *const *b_re,
+                          const double *const *b_im, double *const *x_re, double *const *x_im, int where,
+                          hz_solve_info *info, double *resid);
+
+/* Switch the operator to the Combo formulation (new_HelmholtzKernelCombo,
+ * HelmholtzKernel.c:173-610) before hz_build: points on the annulus
+ * o->delta0 <= |d| <= o->epsilon (hz_dense_opts_default(HZ_DENSE_COMBO) gives
+ * the driver's [0.1 H, sqrt(H)]), weights SineWeight (o->sine) or PolyWeight,
+ * operator A = -i eta (dG/dn_x - 1/2) + d^2G/dn_x dn_y at offset points,
+ * applied matrix free in FP64 (hz_matvec, hz_solve with HZ_PREC_F64; the FP32
+ * sweeps, multi right-hand-side and gradient entries are not available for it).
+ * hz_eval with HZ_COMBO_LAYER evaluates the field.  o = NULL switches back. */
+HZ_API int hz_set_combo(hz_operator *op, const hz_dense_opts *o);
 
 /* Number of kernel launches made by this library in this process (graph
  * launches count their kernels), for launch accounting. */

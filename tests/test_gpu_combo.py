@@ -1,0 +1,142 @@
+"""The Combo formulation as a matrix-free FP64 operator (hz_set_combo).
+
+* On the reference's own configuration (golden fixture ref_neumann_dense_n16:
+  annulus [0.1 H, sqrt(H)]) its points and arrays are the reference's
+  new_HelmholtzKernelCombo rows (x*, normals, regularisation bit-exact, the
+  SineWeight results 1e-14 relative), and A p equals the reference's dense
+  matrix times p to 1e-12 (A^H p: the GPU dense matrix's conjugate transpose).
+* That configuration is not solvable: SineWeight (functions.c:864) is
+  exp(0.5/((t - 0.1)(t - 1))) with its inner bound fixed at 0.1, and the
+  driver's annulus has delta0/epsilon0 = 0.1 sqrt(H) < 0.1, so the weight
+  overflows (to ~1e240) for 0.1 sqrt(H) < |d|/epsilon0 < 0.1.  The solves use
+  delta0 = 0.1 epsilon0, where the weight vanishes below 0.1 as intended:
+  BiCGSTAB, BiCG and GMRES on the exterior-monopole Neumann data
+  (cal_partialu at x*) give the dense solution (numpy) to 1e-8, and
+  Combo_NeumannTest's field (HZ_COMBO_LAYER) equals the numpy restatement of
+  large3Dexample2.c:1975-2055 to 1e-12; at N = 32 the field at
+  (1.5, 0.3, 0.2) is within 3 % of the exact -e^{ikr}/(kr) in modulus
+  (1.4 % measured; 25 % at N = 24, 43 % at N = 16).
+"""
+import json
+
+import numpy as np
+import pytest
+
+from conftest import golden, rel_err
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def combo(hz):
+    g = golden("ref_neumann_dense_n16")
+    m = json.loads(str(g["meta"]))
+    p = hz.params(m["N"], m["wave"], int_l=m["int_l"], int_u=m["int_u"], factor=m["factor"],
+                  tau_factor=m["tau_factor"], dirichlet=m["dirichlet"], interior=m["interior"])
+    f = m["flags"]
+    o = hz.dense_opts(hz.DENSE_COMBO, p, delta0=m["delta0"], epsilon=m["epsilon0"], wavenum=m["wave"], eta=m["eta"],
+                      poly=f["poly"], sine=f["sine"], onesided=f["combo_onesided"], combo_interior=f["combo_interior"])
+    op = hz.Operator(p)
+    op.set_combo(o)
+    op.set_distance(g["d"])
+    op.build()
+    yield op, g, m, p, o
+    op.close()
+
+
+def test_combo_points_are_the_reference_rows(hz, combo):
+    op, g, m, p, o = combo
+    ref = g["combo_pts"]
+    assert op.n == m["n_combo"]
+    t = op.tube()
+    R = hz.DENSE_ROWS
+    xs = np.stack([ref[R.index("xs")], ref[R.index("ys")], ref[R.index("zs")]], 1)
+    nrm = np.stack([ref[R.index("gx")], ref[R.index("gy")], ref[R.index("gz")]], 1)
+    assert np.array_equal(t["xs"].reshape(-1, 3), xs)
+    assert np.array_equal(t["nrm"].reshape(-1, 3), nrm)
+    assert np.array_equal(t["reg"], ref[R.index("reg")])
+    assert rel_err(t["w"], ref[R.index("sineres")]) <= 1e-14
+
+
+def test_combo_matvec_vs_reference_dense(hz, combo):
+    op, g, m, p, o = combo
+    v = g["combo_v"]
+    assert rel_err(op.matvec(v), g["combo_Kv"]) <= 1e-12
+    pts, K1, K2, rc = hz.dense_assemble(hz.DENSE_COMBO, p, o, g["d"])
+    K = K2 if m["flags"]["sine"] else K1
+    assert rel_err(op.matvec(v, adjoint=True), K.conj().T @ v) <= 1e-12
+    q, qt = op.matvec_pair(v, v)
+    assert rel_err(q, K @ v) <= 1e-12 and rel_err(qt, K.conj().T @ v) <= 1e-12
+
+
+def combo_field_numpy(t, sigma, x, k, eta, tau):
+    """large3Dexample2.c:1975-2055 in numpy (sources: x*, n, reg, weight)."""
+    xs = t["xs"].reshape(-1, 3)
+    n = t["nrm"].reshape(-1, 3)
+    d = x[None, :] - xs
+    rho = np.linalg.norm(d, axis=1)
+    inner = np.sum(d * n, axis=1)
+    f1 = 4 * np.pi * rho
+    f2 = f1 * rho
+    pr = np.where(rho > tau, (np.cos(k * rho) / rho + k * np.sin(k * rho)) * inner / f2, t["reg"])
+    pi = np.where(rho > tau, (np.sin(k * rho) / rho - k * np.cos(k * rho)) * inner / f2, 0.0)
+    kr = pr + eta * np.sin(k * rho) / f1
+    ki = pi - eta * np.cos(k * rho) / f1
+    return np.sum((kr + 1j * ki) * sigma * t["w"])
+
+
+def solvable_combo(hz, N, k=2.0):
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    p = hz.params(N, k)  # reference defaults: [-2,2]^3, FACTOR 2, Neumann, exterior
+    d = G.sphere(N, radius=1.0, center=(0.013, 0.021, 0.007), int_l=-2.0, int_u=2.0)
+    eps0 = np.sqrt(4.0 / N)
+    o = hz.dense_opts(hz.DENSE_COMBO, p, delta0=0.1 * eps0, epsilon=eps0, wavenum=k, eta=-1.0)
+    op = hz.Operator(p)
+    op.set_combo(o)
+    op.set_distance(d)
+    op.build()
+    return op, p, o, d
+
+
+@pytest.mark.parametrize("method", ["bicgstab", "bicg", "gmres"])
+def test_combo_monopole_solve_and_field(hz, method):
+    k = 2.0
+    op, p, o, d = solvable_combo(hz, 24, k)
+    b = op.rhs_point_source(np.zeros(3), hz.RHS_MONOPOLE_NEUMANN)
+    meth = {"bicgstab": hz.BICGSTAB, "bicg": hz.BICG, "gmres": hz.GMRES}[method]
+    x, info = op.solve(b, method=meth, precision=hz.PREC_F64, tol=1e-11, maxit=2000, restart=60)
+    assert info["resid"] < 1e-10
+    pts, K1, K2, rc = hz.dense_assemble(hz.DENSE_COMBO, p, o, d)
+    xd = np.linalg.solve(K2, b)
+    assert rel_err(x, xd) < 1e-8
+    rx = np.array([1.5, 0.3, 0.2])
+    u = op.evaluate(rx[None, :], x, hz.COMBO_LAYER)[0]
+    tau = p.tau_factor * 4.0 / 24
+    un = combo_field_numpy(op.tube(), x, rx, k, -1.0, tau)
+    assert abs(u - un) <= 1e-12 * abs(un)
+    op.close()
+
+
+def test_combo_monopole_kat(hz):
+    k = 2.0
+    op, p, o, d = solvable_combo(hz, 32, k)
+    b = op.rhs_point_source(np.zeros(3), hz.RHS_MONOPOLE_NEUMANN)
+    x, info = op.solve(b, method=hz.GMRES, precision=hz.PREC_F64, tol=1e-11, maxit=2000, restart=60)
+    assert info["resid"] < 1e-10
+    rx = np.array([[1.5, 0.3, 0.2]])
+    u = op.evaluate(rx, x, hz.COMBO_LAYER)[0]
+    r = np.linalg.norm(rx)
+    ue = -np.exp(1j * k * r) / (k * r)
+    assert abs(abs(u) - abs(ue)) / abs(ue) < 0.03
+    op.close()
+
+
+def test_combo_guards(hz, combo):
+    op, g, m, p, o = combo
+    v = g["combo_v"]
+    with pytest.raises(hz.HzError):
+        op.matvec(v, precision=hz.PREC_F32)
+    with pytest.raises(hz.HzError):
+        op.solve(v, precision=hz.PREC_F32_REFINED)
+    with pytest.raises(hz.HzError):
+        op.evaluate(np.array([[1.5, 0.3, 0.2]]), v, hz.SINGLE_LAYER)
