@@ -73,6 +73,12 @@ def parse():
                     help="--solve: torus (the step workload) or the ellipsoid (0.7,0.5,0.4) level set "
                          "reinitialised on the device before the build")
     ap.add_argument("--reinit-iters", type=int, default=60, help="--solve --shape ellipsoid: TVD-RK2 steps")
+    ap.add_argument("--plane-waves", type=int, default=0,
+                    help="instead of the step benchmark: solve this many incident plane waves (Fibonacci-sphere "
+                         "directions) on the torus with the multi right-hand-side solver and report the times")
+    ap.add_argument("--batch", type=int, default=0,
+                    help="instead of the step benchmark: solve this many seeded ellipsoids (semi-axes U[0.2,0.7], "
+                         "grids 64^3-192^3) as one batch and one after another, and report both times")
     ap.add_argument("--sweep-variant", type=int, default=-1,
                     help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
@@ -409,14 +415,124 @@ def run_solve(a, local):
     return 0
 
 
+def run_plane_waves(a):
+    """Many incident fields on one surface: one kernel evaluation per pair
+    serves 8 right-hand sides (hz_solve_multi), against single solves."""
+    import numpy as np
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    N, wave, R = a.N, a.wave, a.plane_waves
+    d = G.torus(N, R=0.6, r=0.25, int_l=-1.0, int_u=1.0)
+    p = hz.params(N, wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1)
+    out = {"mode": "plane_waves"}
+    with hz.Operator(p) as op:
+        op.set_distance(d)
+        n = op.build()
+        cfg = op.autotune()[0]
+        dirs = G.fibonacci_sphere(R)
+        B = op.rhs_plane_waves(dirs, hz.RHS_POINT_DIRICHLET)
+        out["config"] = {"workload": "torus R=0.6 r=0.25 on %d^3 over [-1,1]^3, tube |phi|<=3h, k=%g, %d incident "
+                                     "plane waves e^{ik d.x} (Dirichlet data), directions on a Fibonacci sphere"
+                                     % (N, wave, R), "N": N, "n_tube": n, "wave": wave, "nrhs": R,
+                         "sweep_variant": cfg, "rhs_per_kernel_pass": 8}
+        # products: R right-hand sides through the multi-RHS sweep vs R single FP32 products
+        op.matvec_multi(B[:8])
+        t0 = time.perf_counter()
+        op.matvec_multi(B)
+        t_multi = time.perf_counter() - t0
+        t0 = time.perf_counter()
+        for r in range(min(R, 8)):
+            op.matvec(B[r], precision=hz.PREC_F32)
+        t_single = (time.perf_counter() - t0) / min(R, 8) * R
+        out["products"] = {"multi_s": t_multi, "single_s_for_all": t_single, "speedup": t_single / t_multi,
+                           "pairs_x_rhs_per_s_multi": float(n) * n * R / t_multi,
+                           "note": "wall time incl. host<->device copies of the vectors"}
+        # solves: all R in lockstep (FP32 + FP64 refinement) vs one refined BiCGSTAB solve per field
+        X, info, res = op.solve_multi(B, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
+        out["multi_solve"] = dict(info, max_resid=float(np.max(res)))
+        nsingle = min(R, 4)
+        t0 = time.perf_counter()
+        errs = []
+        for r in range(nsingle):
+            x, i1 = op.solve(B[r], method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
+            errs.append(float(np.max(np.abs(x - X[r])) / np.max(np.abs(x))))
+        t_one = (time.perf_counter() - t0) / nsingle
+        out["single_solves"] = {"seconds_per_field": t_one, "fields_timed": nsingle,
+                                "seconds_for_all_extrapolated": t_one * R,
+                                "max_rel_diff_vs_multi": max(errs)}
+        out["multi_solve_speedup_vs_single_extrapolated"] = t_one * R / info["seconds"]
+    print(json.dumps(out))
+    sys.stdout.flush()
+    return 0
+
+
+def run_batch(a):
+    """An uneven batch of ellipsoids solved together (hz_batch_solve: one
+    persistent FP32 launch per product over all surfaces) against the same
+    solves one after another."""
+    import numpy as np
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    rng = np.random.default_rng(2024)
+    count, wave = a.batch, a.wave
+    grids = [64, 96, 128, 160, 192]
+    ops, cases = [], []
+    t0 = time.perf_counter()
+    for i in range(count):
+        axes = tuple(float(x) for x in rng.uniform(0.2, 0.7, 3))
+        # the 3h tube must keep the WENO stencils off the medial surface:
+        # h <= min axis / 7
+        need = int(np.ceil(14.0 / min(axes) / 8.0)) * 8
+        N = max(int(rng.choice(grids)), need)
+        H = 2.0 / N
+        phi = G.ellipsoid_levelset(N, axes=axes)
+        d = hz.reinitialize(phi, N, H, 40)
+        op = hz.Operator(hz.params(N, wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1))
+        op.set_distance(d)
+        n = op.build()
+        ops.append(op)
+        cases.append({"axes": [round(x, 4) for x in axes], "N": N, "n_tube": n})
+    build_s = time.perf_counter() - t0
+    bs = [op.rhs_point_source(np.array([0.02, 0.01, 0.0]), hz.RHS_POINT_DIRICHLET) for op in ops]
+    out = {"mode": "batch", "config": {"workload": "%d ellipsoids, semi-axes U[0.2,0.7] (seed 2024), level sets "
+                                                 "reinitialised on the device, grids 64^3-192^3 over [-1,1]^3, tube "
+                                                 "|phi|<=3h, k=%g, Dirichlet point source at (0.02,0.01,0)"
+                                                 % (count, wave), "surfaces": cases, "wave": wave,
+                                       "build_s": build_s}}
+    with hz.Batch(ops) as b:
+        out["config"]["batch_variant"] = b.autotune()[0]
+        xs, info, res = b.solve(bs, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
+        out["batch_solve"] = dict(info, max_resid=float(np.max(res)))
+    t0 = time.perf_counter()
+    errs, its = [], 0
+    for op, rhs, x in zip(ops, bs, xs):
+        op.autotune()
+        x1, i1 = op.solve(rhs, method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
+        its += i1["iterations"]
+        errs.append(float(np.max(np.abs(x1 - x)) / np.max(np.abs(x1))))
+    out["sequential_solves"] = {"seconds": time.perf_counter() - t0, "iterations": its,
+                                "max_rel_diff_vs_batch": max(errs),
+                                "note": "includes each operator's untimed-in-batch autotune"}
+    out["batch_speedup"] = out["sequential_solves"]["seconds"] / info["seconds"]
+    for op in ops:
+        op.close()
+    print(json.dumps(out))
+    sys.stdout.flush()
+    return 0
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
-    if a.solve:
+    if a.solve or a.plane_waves or a.batch:
         import torch
         torch.cuda.set_device(local)
+        if a.plane_waves:
+            return run_plane_waves(a)
+        if a.batch:
+            return run_batch(a)
         return run_solve(a, local)
     return run_gb300(a, rank, world, local)
 

@@ -93,6 +93,8 @@ SIGNATURES = {
     "hz_get_stream": ([_vp], _vp),
     "hz_set_distance": ([_vp, _vp, C.c_int], C.c_int),
     "hz_set_combo": ([_vp, _vp], C.c_int),
+    "hz_shape_gradient": ([_vp, C.POINTER(SolveOpts), _vp, C.c_int64, _vp, _vp, _vp, C.POINTER(C.c_double), _vp,
+                           C.c_int, C.POINTER(SolveInfo)], C.c_int),
     "hz_batch_create": ([C.POINTER(_vp), C.c_int, C.POINTER(_vp)], C.c_int),
     "hz_batch_destroy": ([_vp], None),
     "hz_batch_autotune": ([_vp, C.POINTER(C.c_int), C.POINTER(C.c_double)], C.c_int),
@@ -238,6 +240,19 @@ class Operator:
 
     def set_stream(self, stream_handle):
         _check(load().hz_set_stream(self.h, stream_handle))
+
+    def shape_gradient(self, src, receivers, target, opts=None, **kw):
+        """(J, dJ/dphi on the grid, info) for point-source Dirichlet data."""
+        opts = opts if opts is not None else solve_opts(**kw)
+        rx = _f64(receivers).reshape(-1, 3)
+        tr, ti = _f64(np.asarray(target).real), _f64(np.asarray(target).imag)
+        S = self.p.N + 1
+        g = np.zeros((S, S, S))
+        J = C.c_double()
+        info = SolveInfo()
+        _check(load().hz_shape_gradient(self.h, C.byref(opts), _ptr(_f64(src)), rx.shape[0], _ptr(rx), _ptr(tr),
+                                        _ptr(ti), C.byref(J), _ptr(g), HZ_HOST, C.byref(info)))
+        return J.value, g, info.as_dict()
 
     def set_combo(self, opts):
         """Switch to the Combo formulation (before build); opts a DenseOpts

@@ -33,6 +33,7 @@ UNITS = {
     "adjoint.cu": [],
     "combo.cu": [],
     "batch.cu": [],
+    "shape_grad.cu": [],
     "capi.cu": [],
     "peaks.cu": [],
     "noalloc.cu": [],

@@ -1219,6 +1219,81 @@ int hz_misfit_gradient(hz_operator *op, const hz_solve_opts *opts_in, const doub
     return HZ_OK;
 }
 
+int hz_shape_gradient(hz_operator *op, const hz_solve_opts *opts_in, const double *src, int64_t m, const double *rx,
+                      const double *t_re, const double *t_im, double *J, double *dJ_dphi, int where,
+                      hz_solve_info *info)
+{
+    HZ_TRY(need_classic(op, "hz_shape_gradient"));
+    HZ_TRY(need_built(op));
+    HZ_TRY(where_ok(where));
+    hz_solve_opts o;
+    if (opts_in) o = *opts_in;
+    else hz_solve_opts_default(&o);
+    HZ_TRY(check_opts(o));
+    if (!op->p.dirichlet || m < 1 || !src || !rx || !t_re || !t_im) {
+        set_error("hz_shape_gradient: needs the Dirichlet formulation, receivers, targets and a source");
+        return HZ_ERR_ARG;
+    }
+    HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    cudaStream_t s = op->stream;
+    const int64_t n = op->n;
+    const size_t S = (size_t)op->p.N + 1, nodes = S * S * S;
+    auto t0 = std::chrono::steady_clock::now();
+    DevBuf buf, work;
+    HZ_TRY(buf.ensure((8 * (size_t)n + 9 * (size_t)m + nodes) * sizeof(double)));
+    HZ_TRY(work.ensure(shape_gradient_work_bytes(n, op->p.N)));
+    double *b0 = buf.as<double>(), *b1 = b0 + n, *sg0 = b0 + 2 * n, *sg1 = b0 + 3 * n, *l0 = b0 + 4 * n,
+           *l1 = b0 + 5 * n, *e0 = b0 + 6 * n, *e1 = b0 + 7 * n;
+    double *R = b0 + 8 * n, *T0 = R + 3 * m, *T1 = T0 + m, *U0 = T1 + m, *U1 = U0 + m, *E0 = U1 + m, *E1 = E0 + m;
+    double *phib = E1 + m;
+    HZ_TRY(stage_in(R, rx, 3 * m, where, s));
+    HZ_TRY(stage_in(T0, t_re, m, where, s));
+    HZ_TRY(stage_in(T1, t_im, m, where, s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
+    HZ_TRY(launch_rhs(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), src, op->p.wave,
+                      HZ_RHS_POINT_DIRICHLET, b0, b1, s));
+    hz_solve_info fwd{}, adj{};
+    int status = HZ_OK, status2 = HZ_OK;
+    HZ_TRY(solve_device(op, o, false, b0, b1, sg0, sg1, fwd, status));
+    HZ_TRY(launch_eval(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), sg0, sg1, m, R, op->p.wave, op->tau,
+                       op->p.interior, HZ_DOUBLE_LAYER, U0, U1, s));
+    HZ_TRY(vec_sub(m, U0, U1, T0, T1, E0, E1, s));  // r = u - t
+    HZ_TRY(launch_eval_adjoint(n, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), m, R, E0, E1, op->p.wave,
+                               op->tau, op->p.interior, HZ_DOUBLE_LAYER, e0, e1, s));
+    HZ_TRY(solve_device(op, o, true, e0, e1, l0, l1, adj, status2));
+    HZ_TRY(shape_gradient_device(op->p, op->H, op->eps, op->tau, n, op->idx.as<int64_t>(), op->d.as<double>(),
+                                 op->gx.as<double>(), op->gy.as<double>(), op->gz.as<double>(), op->mc.as<double>(),
+                                 op->gc.as<double>(), op->xs.as<double>(), op->w.as<double>(),
+                                 op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), sg0, sg1, l0, l1, m, R, E0,
+                                 E1, src, work.as<double>(), phib, s));
+    std::vector<double> hr0(m), hr1(m);
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hr0.data(), E0, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(hr1.data(), E1, m * sizeof(double), cudaMemcpyDeviceToHost, s));
+    HZ_TRY(stage_out(dJ_dphi, phib, nodes, where, s));
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+    double jv = 0.0;
+    for (int64_t i = 0; i < m; i++) jv += hr0[i] * hr0[i] + hr1[i] * hr1[i];
+    if (J) *J = jv;
+    int rc = check_device_error(op, "hz_shape_gradient");
+    if (info) {
+        hz_solve_info inf = fwd;
+        inf.iterations = fwd.iterations + adj.iterations;
+        inf.outer = fwd.outer + adj.outer;
+        inf.resid = fwd.resid > adj.resid ? fwd.resid : adj.resid;
+        inf.resid_f64 = fwd.resid_f64 > adj.resid_f64 ? fwd.resid_f64 : adj.resid_f64;
+        inf.pair_evals = fwd.pair_evals + adj.pair_evals + n * n;
+        inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        inf.status = rc != HZ_OK ? rc : (status != HZ_OK ? status : status2);
+        *info = inf;
+    }
+    if (rc != HZ_OK) return rc;
+    if (status != HZ_OK || status2 != HZ_OK) {
+        set_error("solver stopped early (status %d / %d)", status, status2);
+        return status != HZ_OK ? status : status2;
+    }
+    return HZ_OK;
+}
+
 int hz_rhs_point_source(hz_operator *op, const double *src, int kind, double *b_re, double *b_im, int where)
 {
     HZ_TRY(need_built(op));

@@ -161,9 +161,21 @@ int sweep_combo64(int64_t n, double wave, double wavenum, double eta, double tau
 int launch_eval_combo(int64_t n, const double4_32a *pos, const double4_32a *nrm, const double *s_re,
                       const double *s_im, int64_t m, const double *rx, double wave, double tau, double eta,
                       double *u_re, double *u_im, cudaStream_t s);
+// shape_grad.cu: dJ/dphi given sigma, lambda and the receiver residuals
+int shape_gradient_device(const hz_params &p, double H, double eps, double tau, int64_t n, const int64_t *idx,
+                          const double *d, const double *gx, const double *gy, const double *gz, const double *mc,
+                          const double *gc, const double *xs, const double *w, const double4_32a *pos,
+                          const double4_32a *nrm, const double *s_re, const double *s_im, const double *l_re,
+                          const double *l_im, int64_t m, const double *rx, const double *r_re, const double *r_im,
+                          const double *src, double *work, double *phib, cudaStream_t s);
+size_t shape_gradient_work_bytes(int64_t n, int N);
 // stencils.cu
 int launch_grid_stencils(int N, double H, const double *d, double *gx, double *gy, double *gz,
                          double *mc, double *gc, int order, cudaStream_t s);
+// reverse of the grid stencils by local central differences (stencils.cu):
+// phib += the adjoints of gx, gy, gz, mc, gc pulled back to the grid values
+int launch_stencil_adjoint(int N, double H, const double *d, const double *gxb, const double *gyb, const double *gzb,
+                           const double *mcb, const double *gcb, double *phib, int order, double h, cudaStream_t s);
 // reinitialisation (stencils.cu): iters TVD-RK2 steps of dt = cfl*H, in place
 int launch_reinit(int N, double H, double *phi, double *tmp1, double *tmp2, const double *phi0, int iters,
                   double cfl, int order, cudaStream_t s);

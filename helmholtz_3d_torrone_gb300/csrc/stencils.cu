@@ -80,15 +80,30 @@ __device__ void weno(double *dfp, double *dfn, const double *fi, double dx, int 
     *dfn = df - w0 * (aa - 2. * bb + cc) / 3. - (w2 - .5) * (bb - 2. * cc + dd) / 6.;
 }
 
-// Values along one axis through the node: v(m) = d[base + m*stride].
-struct Line {
+// Grid accessors: the grid itself, or the grid with one value moved by
+// delta (the local finite differences of the shape gradient).
+struct GridAcc {
     const double *__restrict__ d;
+    __device__ double operator()(long long q) const { return __ldg(d + q); }
+};
+struct PertAcc {
+    const double *__restrict__ d;
+    long long kq;
+    double delta;
+    __device__ double operator()(long long q) const { return (q == kq) ? __ldg(d + q) + delta : __ldg(d + q); }
+};
+
+// Values along one axis through the node: v(m) = d[base + m*stride].
+template <class A>
+struct Line {
+    A a;
     long long base, stride;
-    __device__ double operator()(int m) const { return __ldg(d + base + (long long)m * stride); }
+    __device__ double operator()(int m) const { return a(base + (long long)m * stride); }
 };
 
 // finite_difference3D.c:220-390; xorder selects XDER2's min_abs argument order.
-__device__ double der2(const Line &L, int c, int N, double H, bool xorder)
+template <class L_>
+__device__ double der2(const L_ &L, int c, int N, double H, bool xorder)
 {
     double DDp, DDc, DDn;
     if (c == 0) return 2.0 * (L(1) - L(0)) / (H * H);
@@ -119,17 +134,16 @@ __device__ double der2(const Line &L, int c, int N, double H, bool xorder)
     return DDc;
 }
 
+template <class A>
 struct Plane {
-    const double *__restrict__ d;
+    A a;
     long long base, sa, sb;
-    __device__ double operator()(int u, int v) const
-    {
-        return __ldg(d + base + (long long)u * sa + (long long)v * sb);
-    }
+    __device__ double operator()(int u, int v) const { return a(base + (long long)u * sa + (long long)v * sb); }
 };
 
 // finite_difference3D.c:393-721 (secondpartialxy/xz/yz).
-__device__ double cross(const Plane &P, int ca, int cb, int N, double H)
+template <class P_>
+__device__ double cross(const P_ &P, int ca, int cb, int N, double H)
 {
     const double coef[3] = {1.0, -4.0, 3.0};
     if ((ca == 0) || (ca == N) || (cb == 0) || (cb == N)) return 0.0;
@@ -169,6 +183,55 @@ __device__ double cross(const Plane &P, int ca, int cb, int N, double H)
     return fin / (4.0 * H * H);
 }
 
+// Gradient (gx, gy, gz) and curvatures (mc, gc) of one node (i, j, k),
+// o = its linear index, from the grid accessor acc.
+template <class A>
+__device__ __forceinline__ void grid_node(const A &acc, int N, double H, int i, int j, int k, long long o, int order,
+                                          bool want_grad, bool want_curv, double out[5])
+{
+    const long long S = N + 1;
+    if (want_grad) {
+        // distance_application3D.c:56-140 with WENO_DX/DY/DZ (weno.c:117-254)
+        const int half = (order == 5) ? 3 : 2;
+        double f[7], Dxp, Dxn, Dyp, Dyn, Dzp, Dzn;
+        for (int m = -half; m <= half; m++) f[m + half] = acc((i * S + mirror(j + m, N)) * S + k);
+        weno(&Dxp, &Dxn, f, H, order);
+        for (int m = -half; m <= half; m++) f[m + half] = acc((mirror(i + m, N) * S + j) * S + k);
+        weno(&Dyp, &Dyn, f, H, order);
+        for (int m = -half; m <= half; m++) f[m + half] = acc((i * S + j) * S + mirror(k + m, N));
+        weno(&Dzp, &Dzn, f, H, order);
+        const double aplus = rmax(0.0, Dxp), aminus = rmin(0.0, Dxp);
+        const double bplus = rmax(0.0, Dxn), bminus = rmin(0.0, Dxn);
+        const double cplus = rmax(0.0, Dyp), cminus = rmin(0.0, Dyp);
+        const double dplus = rmax(0.0, Dyn), dminus = rmin(0.0, Dyn);
+        const double eplus = rmax(0.0, Dzp), eminus = rmin(0.0, Dzp);
+        const double fplus = rmax(0.0, Dzn), fminus = rmin(0.0, Dzn);
+        if (acc(o) > 0.0) {
+            out[0] = (fabs(aminus) > fabs(bplus)) ? aminus : bplus;
+            out[1] = (fabs(cminus) > fabs(dplus)) ? cminus : dplus;
+            out[2] = (fabs(eminus) > fabs(fplus)) ? eminus : fplus;
+        } else {
+            out[0] = (fabs(aplus) > fabs(bminus)) ? aplus : bminus;
+            out[1] = (fabs(cplus) > fabs(dminus)) ? cplus : dminus;
+            out[2] = (fabs(eplus) > fabs(fminus)) ? eplus : fminus;
+        }
+    }
+    if (want_curv) {
+        // distance_application3D.c:35-53
+        const Line<A> Lx{acc, o, S}, Ly{acc, o, S * S}, Lz{acc, o, 1};
+        const double dxx = der2(Lx, j, N, H, true);
+        const double dyy = der2(Ly, i, N, H, false);
+        const double dzz = der2(Lz, k, N, H, false);
+        const double dxy = cross(Plane<A>{acc, o, S * S, S}, i, j, N, H);
+        const double dxz = cross(Plane<A>{acc, o, S, 1}, j, k, N, H);
+        const double dyz = cross(Plane<A>{acc, o, S * S, 1}, i, k, N, H);
+        const double diag = dxx * dyy + dyy * dzz + dxx * dzz;
+        const double crs = dxy * dxy + dyz * dyz + dxz * dxz;
+        out[3] = -0.5 * (dxx + dyy + dzz);
+        out[4] = diag - crs;
+    }
+}
+
 __global__ void __launch_bounds__(256) grid_kernel(int N, double H, const double *__restrict__ d,
                                                    double *__restrict__ gx, double *__restrict__ gy,
                                                    double *__restrict__ gz, double *__restrict__ mc,
@@ -176,54 +239,76 @@ __global__ void __launch_bounds__(256) grid_kernel(int N, double H, const double
 {
     const long long S = N + 1;
     const long long total = S * S * S;
+    const GridAcc acc{d};
     for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
          o += (long long)gridDim.x * blockDim.x) {
         const int k = (int)(o % S);
         const int j = (int)((o / S) % S);
         const int i = (int)(o / (S * S));
+        double out[5];
+        grid_node(acc, N, H, i, j, k, o, order, gx != nullptr, mc != nullptr, out);
         if (gx) {
-            // distance_application3D.c:56-140 with WENO_DX/DY/DZ (weno.c:117-254)
-            const int half = (order == 5) ? 3 : 2;
-            double f[7], Dxp, Dxn, Dyp, Dyn, Dzp, Dzn;
-            for (int m = -half; m <= half; m++) f[m + half] = __ldg(d + (i * S + mirror(j + m, N)) * S + k);
-            weno(&Dxp, &Dxn, f, H, order);
-            for (int m = -half; m <= half; m++) f[m + half] = __ldg(d + (mirror(i + m, N) * S + j) * S + k);
-            weno(&Dyp, &Dyn, f, H, order);
-            for (int m = -half; m <= half; m++) f[m + half] = __ldg(d + (i * S + j) * S + mirror(k + m, N));
-            weno(&Dzp, &Dzn, f, H, order);
-            const double aplus = rmax(0.0, Dxp), aminus = rmin(0.0, Dxp);
-            const double bplus = rmax(0.0, Dxn), bminus = rmin(0.0, Dxn);
-            const double cplus = rmax(0.0, Dyp), cminus = rmin(0.0, Dyp);
-            const double dplus = rmax(0.0, Dyn), dminus = rmin(0.0, Dyn);
-            const double eplus = rmax(0.0, Dzp), eminus = rmin(0.0, Dzp);
-            const double fplus = rmax(0.0, Dzn), fminus = rmin(0.0, Dzn);
-            double rx, ry, rz;
-            if (__ldg(d + o) > 0.0) {
-                rx = (fabs(aminus) > fabs(bplus)) ? aminus : bplus;
-                ry = (fabs(cminus) > fabs(dplus)) ? cminus : dplus;
-                rz = (fabs(eminus) > fabs(fplus)) ? eminus : fplus;
-            } else {
-                rx = (fabs(aplus) > fabs(bminus)) ? aplus : bminus;
-                ry = (fabs(cplus) > fabs(dminus)) ? cplus : dminus;
-                rz = (fabs(eplus) > fabs(fminus)) ? eplus : fminus;
-            }
-            gx[o] = rx;
-            gy[o] = ry;
-            gz[o] = rz;
+            gx[o] = out[0];
+            gy[o] = out[1];
+            gz[o] = out[2];
         }
         if (mc) {
-            // distance_application3D.c:35-53
-            const Line Lx{d, o, S}, Ly{d, o, S * S}, Lz{d, o, 1};
-            const double dxx = der2(Lx, j, N, H, true);
-            const double dyy = der2(Ly, i, N, H, false);
-            const double dzz = der2(Lz, k, N, H, false);
-            const double dxy = cross(Plane{d, o, S * S, S}, i, j, N, H);
-            const double dxz = cross(Plane{d, o, S, 1}, j, k, N, H);
-            const double dyz = cross(Plane{d, o, S * S, 1}, i, k, N, H);
-            const double diag = dxx * dyy + dyy * dzz + dxx * dzz;
-            const double crs = dxy * dxy + dyz * dyz + dxz * dxz;
-            mc[o] = -0.5 * (dxx + dyy + dzz);
-            gc[o] = diag - crs;
+            mc[o] = out[3];
+            gc[o] = out[4];
+        }
+    }
+}
+
+// Reverse of the grid stencils by local central differences: every node p
+// with a nonzero adjoint (gxb, gyb, gzb, mcb, gcb) of its outputs adds, to
+// every grid value q that its stencils read,
+//   phib[q] += sum_out adj_out * (out(phi + h e_q) - out(phi - h e_q)) / (2h).
+// The reads: the three axis lines +-3 (mirrored, WENO and second
+// differences) and the three coordinate planes +-2 (cross derivatives).
+__global__ void __launch_bounds__(128) stencil_adjoint_kernel(int N, double H, const double *__restrict__ d,
+                                                              const double *__restrict__ gxb,
+                                                              const double *__restrict__ gyb,
+                                                              const double *__restrict__ gzb,
+                                                              const double *__restrict__ mcb,
+                                                              const double *__restrict__ gcb, double *phib, int order,
+                                                              double h)
+{
+    const long long S = N + 1;
+    const long long total = S * S * S;
+    for (long long o = blockIdx.x * (long long)blockDim.x + threadIdx.x; o < total;
+         o += (long long)gridDim.x * blockDim.x) {
+        const double ab[5] = {gxb[o], gyb[o], gzb[o], mcb[o], gcb[o]};
+        const bool want_grad = ab[0] != 0.0 || ab[1] != 0.0 || ab[2] != 0.0;
+        const bool want_curv = ab[3] != 0.0 || ab[4] != 0.0;
+        if (!want_grad && !want_curv) continue;
+        const int k = (int)(o % S), j = (int)((o / S) % S), i = (int)(o / (S * S));
+        long long deps[96];
+        int nd = 0;
+        auto add = [&](long long q) {
+            for (int t = 0; t < nd; t++)
+                if (deps[t] == q) return;
+            deps[nd++] = q;
+        };
+        for (int m = -3; m <= 3; m++) {
+            add((i * S + mirror(j + m, N)) * S + k);
+            add((mirror(i + m, N) * S + j) * S + k);
+            add((i * S + j) * S + mirror(k + m, N));
+        }
+        if (want_curv)
+            for (int u = -2; u <= 2; u++)
+                for (int v = -2; v <= 2; v++) {
+                    if (i + u >= 0 && i + u <= N && j + v >= 0 && j + v <= N) add(((i + u) * S + j + v) * S + k);
+                    if (j + u >= 0 && j + u <= N && k + v >= 0 && k + v <= N) add((i * S + j + u) * S + k + v);
+                    if (i + u >= 0 && i + u <= N && k + v >= 0 && k + v <= N) add(((i + u) * S + j) * S + k + v);
+                }
+        for (int t = 0; t < nd; t++) {
+            double op_[5] = {0, 0, 0, 0, 0}, om[5] = {0, 0, 0, 0, 0};
+            grid_node(PertAcc{d, deps[t], h}, N, H, i, j, k, o, order, want_grad, want_curv, op_);
+            grid_node(PertAcc{d, deps[t], -h}, N, H, i, j, k, o, order, want_grad, want_curv, om);
+            double acc = 0.0;
+#pragma unroll
+            for (int q = 0; q < 5; q++) acc += ab[q] * (op_[q] - om[q]);
+            if (acc != 0.0) atomicAdd(phib + deps[t], acc / (2.0 * h));
         }
     }
 }
@@ -276,6 +361,17 @@ __global__ void __launch_bounds__(256) reinit_stage_kernel(int N, double H, doub
 }
 
 }  // namespace
+
+int launch_stencil_adjoint(int N, double H, const double *d, const double *gxb, const double *gyb, const double *gzb,
+                           const double *mcb, const double *gcb, double *phib, int order, double h, cudaStream_t s)
+{
+    const long long S = N + 1, total = S * S * S;
+    long long b = (total + 127) / 128;
+    if (b > 152LL * 32) b = 152LL * 32;
+    stencil_adjoint_kernel<<<(unsigned)b, 128, 0, s>>>(N, H, d, gxb, gyb, gzb, mcb, gcb, phib, order, h);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
 
 int launch_reinit(int N, double H, double *phi, double *tmp1, double *tmp2, const double *phi0, int iters,
                   double cfl, int order, cudaStream_t s)

@@ -33,7 +33,8 @@ namespace {
 
 struct Args64 {
     int64_t n;
-    double wave, tau, tau2, sg;
+    double wave, tau, tau2;
+    double inv_scale;  // 4 pi sg: the near-field value times this cancels the density prescale
     const double4_32a *pos, *nrm;
     const double4_32a *dens;  // (w_s p_re, w_s p_im, pt_re, pt_im)
     const double *p_re, *p_im, *pt_re, *pt_im;
@@ -41,26 +42,28 @@ struct Args64 {
     unsigned *err;
 };
 
+// dens = scale (w p, pt), scale = sg / (4 pi): the kernel's common factor.
 __global__ void prep64_kernel(int64_t n, const double4_32a *__restrict__ nrm, const double *__restrict__ p_re,
                               const double *__restrict__ p_im, const double *__restrict__ pt_re,
-                              const double *__restrict__ pt_im, double4_32a *__restrict__ dens)
+                              const double *__restrict__ pt_im, double scale, double4_32a *__restrict__ dens)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
-        const double w = nrm[s].w;
+        const double w = nrm[s].w * scale;
         double a = 0, b = 0, c = 0, d = 0;
         if (p_re) {
             a = w * p_re[s];
             b = w * p_im[s];
         }
         if (pt_re) {
-            c = pt_re[s];
-            d = pt_im[s];
+            c = scale * pt_re[s];
+            d = scale * pt_im[s];
         }
         dens[s] = make_double4_32a(a, b, c, d);
     }
 }
 
 constexpr int kSinTable = 128;
+constexpr double kPi64 = 3.14159265358979323846264338328;
 
 // sin and cos of x >= 0 by table lookup + short series (see the header).
 __device__ __forceinline__ void table_sincos(double x, const double2 *tab, double &s, double &c)
@@ -69,10 +72,13 @@ __device__ __forceinline__ void table_sincos(double x, const double2 *tab, doubl
     const double kInvStep = 20.371832715762604;      // 128 / (2 pi)
     const double kStepHi = 0.049087385210441425;     // 2 pi / 128 rounded to 31 significant bits
     const double kStepLo = 1.899093908283185e-12;    // 2 pi / 128 - kStepHi
-    const double m = rint(x * kInvStep);
+    // nearest integer m to x * 128/(2 pi) (below 2^51): add and remove 1.5 2^52;
+    // the table index is the low word of the sum
+    const double xm = fma(x, kInvStep, 6755399441055744.0);
+    const double m = xm - 6755399441055744.0;
     double r = fma(-m, kStepHi, x);
     r = fma(-m, kStepLo, r);
-    const double2 t = tab[((int)m) & (kSinTable - 1)];
+    const double2 t = tab[__double2loint(xm) & (kSinTable - 1)];
     const double z = r * r;
     // sin r = r - r^3/3! + r^5/5! - r^7/7!,  cos r = 1 - r^2/2! + r^4/4! - r^6/6!
     const double ps = fma(fma(z, -1.0 / 5040.0, 1.0 / 120.0), z, -1.0 / 6.0);
@@ -96,7 +102,6 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
         sincospi((double)i / (kSinTable / 2), &si, &co);
         tab[i] = make_double2(si, co);
     }
-    const double c4 = 1. / (4. * 3.14159265358979323846264338328);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < a.n;
     double4_32a tp = make_double4_32a(0, 0, 0, 0), tn = make_double4_32a(0, 0, 0, 0);
@@ -151,25 +156,26 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
                     const double rho = r2 * rec;
                     double S, C;
                     table_sincos(a.wave * rho, tab, S, C);
+                    // sg / (4 pi) rides on the densities
                     const double eS = S * rec, eC = C * rec;
-                    const double denom = c4 * rec * rec;
+                    const double denom = rec * rec;
                     const double ct1 = -1. * (a.wave * S + eC) * denom;
                     const double ct2 = (a.wave * C - eS) * denom;
                     if (MODE & SWEEP_A) {
                         const double in = DIR ? (xmy1 * sn_.x + xmy2 * sn_.y + xmy3 * sn_.z)
                                               : (xmy1 * tn.x + xmy2 * tn.y + xmy3 * tn.z);
-                        vAr = a.sg * ct1 * in;
-                        vAi = a.sg * ct2 * in;
+                        vAr = ct1 * in;
+                        vAi = ct2 * in;
                     }
                     if (MODE & SWEEP_AH) {
                         const double in = -(DIR ? (xmy1 * tn.x + xmy2 * tn.y + xmy3 * tn.z)
                                                 : (xmy1 * sn_.x + xmy2 * sn_.y + xmy3 * sn_.z));
-                        vHr = a.sg * ct1 * in;
-                        vHi = -(a.sg * ct2 * in);
+                        vHr = ct1 * in;
+                        vHi = -(ct2 * in);
                     }
                 } else {
-                    vAr = DIR ? sp_.w : tp.w;
-                    vHr = DIR ? tp.w : sp_.w;
+                    vAr = (DIR ? sp_.w : tp.w) * a.inv_scale;
+                    vHr = (DIR ? tp.w : sp_.w) * a.inv_scale;
                     vAi = 0.0;
                     vHi = 0.0;
                 }
@@ -226,7 +232,8 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
         long long b = (c.n + 255) / 256;
         if (b > sms * 8) b = sms * 8;
         prep64_kernel<<<(unsigned)b, 256, 0, s>>>(c.n, r.nrm, useA ? p_re : nullptr, useA ? p_im : nullptr,
-                                                  useH ? pt_re : nullptr, useH ? pt_im : nullptr, dens);
+                                                  useH ? pt_re : nullptr, useH ? pt_im : nullptr,
+                                                  ((c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi64), dens);
         HZ_CHECK_LAUNCH();
     }
     Args64 a;
@@ -234,7 +241,7 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     a.wave = c.wave;
     a.tau = c.tau;
     a.tau2 = c.tau * c.tau;
-    a.sg = (c.interior == 1) ? -1.0 : 1.0;
+    a.inv_scale = ((c.interior == 1) ? -1.0 : 1.0) * (4.0 * kPi64);
     a.pos = r.pos;
     a.nrm = r.nrm;
     a.dens = dens;

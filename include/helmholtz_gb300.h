@@ -210,6 +210,22 @@ HZ_API int hz_misfit_gradient(hz_operator *op, const hz_solve_opts *opts, const 
                               const double *t_re, const double *t_im, double *J, double *g_re,
                               double *g_im, double *dJ_dk, double *dJ_dw, int where, hz_solve_info *info);
 
+/* Misfit gradient with respect to the distance-grid values (the shape):
+ * J = sum_m |u(x_m) - t_m|^2 for the Dirichlet formulation with double-layer
+ * receivers and point-source data g = e^{ik|x*-src|}/(4 pi |x*-src|) at the
+ * projected points (src: 3 doubles, host memory), and dJ/dphi at every grid
+ * node ((N+1)^3 doubles).  One forward and one adjoint solve (opts as in
+ * hz_solve) give the sensitivities to every tube point's projection,
+ * normal, weight and regularisation factor (an FP64 pair sweep); they are
+ * pulled back through the projection, the trilinear interpolations, the
+ * normalisations, delta_eps and the Jacobian exactly, and through the
+ * WENO-gradient and curvature stencils by local central differences
+ * (step 1e-7).  Tube membership changes (|phi| crossing eps) are not
+ * differentiated.  Needs p.dirichlet = 1. */
+HZ_API int hz_shape_gradient(hz_operator *op, const hz_solve_opts *opts, const double *src, int64_t m,
+                             const double *rx, const double *t_re, const double *t_im, double *J, double *dJ_dphi,
+                             int where, hz_solve_info *info);
+
 /* Boundary data at the projected points (see HZ_RHS_*). src: 3 doubles. */
 HZ_API int hz_rhs_point_source(hz_operator *op, const double *src, int kind, double *b_re, double *b_im,
                         int where);
