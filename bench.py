@@ -503,16 +503,19 @@ def run_batch(a):
         out["config"]["batch_variant"] = b.autotune()[0]
         xs, info, res = b.solve(bs, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
         out["batch_solve"] = dict(info, max_resid=float(np.max(res)))
-    t0 = time.perf_counter()
-    errs, its = [], 0
-    for op, rhs, x in zip(ops, bs, xs):
+    for op in ops:
         op.autotune()
+    t0 = time.perf_counter()
+    errs, its, pairs = [], 0, 0
+    for op, rhs, x in zip(ops, bs, xs):
         x1, i1 = op.solve(rhs, method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
         its += i1["iterations"]
+        pairs += i1["pair_evals"]
         errs.append(float(np.max(np.abs(x1 - x)) / np.max(np.abs(x1))))
-    out["sequential_solves"] = {"seconds": time.perf_counter() - t0, "iterations": its,
+    out["sequential_solves"] = {"seconds": time.perf_counter() - t0, "iterations": its, "pair_evals": pairs,
                                 "max_rel_diff_vs_batch": max(errs),
-                                "note": "includes each operator's untimed-in-batch autotune"}
+                                "note": "one refined BiCGSTAB solve per surface, each with its own autotuned "
+                                        "sweep variant (autotune untimed, as the batch's)"}
     out["batch_speedup"] = out["sequential_solves"]["seconds"] / info["seconds"]
     for op in ops:
         op.close()

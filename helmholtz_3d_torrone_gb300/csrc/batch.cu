@@ -6,8 +6,11 @@
 // R independent BiCGSTAB solves.  The FP32 product is one persistent
 // stream-K launch over the concatenated (operator, target block, source
 // tile) units of all operators (sweep_f32.cu, sweep32_batch_kernel), and the
-// whole BiCGSTAB iteration is captured once as a CUDA graph.  The FP64
-// products (refinement residuals) run one FP64 sweep per operator.
+// whole BiCGSTAB iteration is captured once as a CUDA graph.  A system that
+// has converged leaves the batch: the launch is re-described over the
+// operators whose columns still iterate (and the graph captured again), and
+// the refinement neither re-solves it nor recomputes its FP64 residual.  The
+// FP64 products (refinement residuals) run one FP64 sweep per operator.
 #include "hz_internal.cuh"
 #include "krylov.cuh"
 #include "krylov_multi.cuh"
@@ -31,6 +34,12 @@ struct hz_batch {
     int shape = 1;  // FP32 batch sweep shape (hz_batch_autotune)
     DevBuf desc;    // kBatchShapes descriptor arrays
     int64_t units[kBatchShapes] = {}, blocks[kBatchShapes] = {};
+    std::vector<Batch32Item> items;
+    // the FP32 launch over a subset of the operators (sub_n > 0)
+    DevBuf desc_sub;
+    int sub_n = 0, sub_shape = -1;
+    int64_t sub_units = 0, sub_blocks = 0;
+    uint64_t sub_gen = 0;
     DevBuf partial;
     size_t partial_bytes = 0;
     KrylovMulti multi;
@@ -41,32 +50,67 @@ namespace {
 
 struct BatchF32 final : MultiOp {
     hz_batch *b;
+    bool sub = false;  // launch over b->desc_sub
     explicit BatchF32(hz_batch *bb) : b(bb) {}
     int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im, cudaStream_t s) override
     {
         (void)R;
+        if (sub && b->sub_shape == b->shape)
+            return sweep_f32_batch(b->shape, b->desc_sub.ptr, b->sub_n, b->R, b->sub_units, b->sub_blocks,
+                                   b->partial.as<double4_32a>(), b->partial_bytes, p_re, p_im, q_re, q_im, b->nmax,
+                                   b->max_npad, s, nullptr, nullptr);
         const size_t db = batch32_desc_bytes(b->R);
-        return sweep_f32_batch(b->shape, b->desc.as<char>() + (size_t)b->shape * db, b->R, b->units[b->shape],
+        return sweep_f32_batch(b->shape, b->desc.as<char>() + (size_t)b->shape * db, b->R, b->R, b->units[b->shape],
                                b->blocks[b->shape], b->partial.as<double4_32a>(), b->partial_bytes, p_re, p_im, q_re,
                                q_im, b->nmax, b->max_npad, s, nullptr, nullptr);
     }
-    uint64_t key() const override { return ((uint64_t)(uintptr_t)b << 4) ^ (uint64_t)(b->shape + 1); }
+    uint64_t key() const override
+    {
+        const uint64_t g = sub ? b->sub_gen : 0;
+        return ((uint64_t)(uintptr_t)b << 4) ^ (uint64_t)(b->shape + 1) ^ (g << 40);
+    }
+    int restrict_to(const std::vector<int> &cols, cudaStream_t s) override
+    {
+        if ((int)cols.size() == b->R) {
+            sub = false;
+            return HZ_OK;
+        }
+        sub = false;
+        b->sub_n = 0;
+        b->sub_shape = -1;
+        HZ_TRY(batch32_describe(b->items.data(), (int)cols.size(), b->shape, b->desc_sub.ptr, b->sub_units,
+                                b->sub_blocks, s, cols.data()));
+        b->sub_n = (int)cols.size();
+        b->sub_shape = b->shape;
+        b->sub_gen++;
+        sub = true;
+        return HZ_OK;
+    }
 };
 
 struct BatchF64 final : MultiOp {
     hz_batch *b;
+    std::vector<int> cols;  // empty: every operator
     explicit BatchF64(hz_batch *bb) : b(bb) {}
     int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im, cudaStream_t s) override
     {
         (void)R;
         HZ_CHECK_CUDA(cudaMemsetAsync(q_re, 0, (size_t)b->R * b->nmax * sizeof(double), s));
         HZ_CHECK_CUDA(cudaMemsetAsync(q_im, 0, (size_t)b->R * b->nmax * sizeof(double), s));
-        for (int r = 0; r < b->R; r++) {
+        const int m = cols.empty() ? b->R : (int)cols.size();
+        for (int i = 0; i < m; i++) {
+            const int r = cols.empty() ? i : cols[i];
             hz_operator *op = b->ops[r];
             const size_t off = (size_t)r * b->nmax;
             HZ_TRY(sweep_f64(sweep_const(op), rec64(op), SWEEP_A, p_re + off, p_im + off, nullptr, nullptr, q_re + off,
                              q_im + off, nullptr, nullptr, op->scratch.as<double2>(), s));
         }
+        return HZ_OK;
+    }
+    int restrict_to(const std::vector<int> &c, cudaStream_t s) override
+    {
+        (void)s;
+        cols = c;
         return HZ_OK;
     }
 };
@@ -146,7 +190,9 @@ int hz_batch_create(hz_operator *const *ops, int count, hz_batch **out)
     int rc = cudaSetDevice(b->device) == cudaSuccess ? HZ_OK : HZ_ERR_CUDA;
     const size_t db = batch32_desc_bytes(count);
     if (rc == HZ_OK) rc = b->desc.ensure(kBatchShapes * db);
-    std::vector<Batch32Item> items(count);
+    if (rc == HZ_OK) rc = b->desc_sub.ensure(db);
+    std::vector<Batch32Item> &items = b->items;
+    items.resize(count);
     for (int r = 0; r < count && rc == HZ_OK; r++) {
         hz_operator *op = ops[r];
         items[r].c = sweep_const(op);
@@ -190,7 +236,7 @@ int hz_batch_autotune(hz_batch *b, int *chosen, double *ms_per_sweep)
     for (int k = 0; k < kBatchShapes && rc == HZ_OK; k++) {
         float ms_min = 1e30f;
         for (int rep = 0; rep < 2 && rc == HZ_OK; rep++) {
-            rc = sweep_f32_batch(k, b->desc.as<char>() + (size_t)k * db, b->R, b->units[k], b->blocks[k],
+            rc = sweep_f32_batch(k, b->desc.as<char>() + (size_t)k * db, b->R, b->R, b->units[k], b->blocks[k],
                                  b->partial.as<double4_32a>(), b->partial_bytes, v, v + tot, v + 2 * tot, v + 3 * tot,
                                  b->nmax, b->max_npad, s, e0, e1);
             if (rc == HZ_OK && cudaEventSynchronize(e1) == cudaSuccess) {
@@ -281,18 +327,24 @@ int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts_in, const double *cons
     HZ_TRY(b->multi.reserve(nm, R));
     std::vector<double> res(R, 0.0);
     int iters = 0, outer = 0;
-    long long pairs = 0, sq = 0;
-    for (hz_operator *op : b->ops) sq += (long long)op->n * op->n;
+    long long pairs = 0;
+    std::vector<int> cit;
+    auto pairs_of = [&](const std::vector<int> &its, int products) {
+        long long p = 0;
+        for (int r = 0; r < R; r++) p += (long long)products * its[r] * b->ops[r]->n * b->ops[r]->n;
+        return p;
+    };
     if (o.precision != HZ_PREC_F32_REFINED) {
         BatchF32 A32(b);
         BatchF64 A64(b);
         MultiOp &A = (o.precision == HZ_PREC_F32) ? static_cast<MultiOp &>(A32) : static_cast<MultiOp &>(A64);
-        HZ_TRY(b->multi.solve(A, B0, B1, o.tol, o.maxit, o.stagnation != 0, s, iters, res));
+        HZ_TRY(b->multi.solve(A, B0, B1, o.tol, o.maxit, o.stagnation != 0, s, iters, res, 0, &cit));
         HZ_CHECK_CUDA(cudaMemcpyAsync(X0, b->multi.re(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
         HZ_CHECK_CUDA(cudaMemcpyAsync(X1, b->multi.im(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        pairs = 2LL * iters * sq;
+        pairs = pairs_of(cit, 2);
     } else {
-        // FP64 iterative refinement of every system: x_r += ||r_r|| A32^{-1}(r_r/||r_r||)
+        // FP64 iterative refinement of every system still above tol:
+        // x_r += ||r_r|| A32^{-1}(r_r/||r_r||)
         BatchF32 A32(b);
         BatchF64 A64(b);
         HZ_TRY(b->small.ensure(vec_partial_bytes() + 64));
@@ -311,25 +363,39 @@ int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts_in, const double *cons
             for (double v : res) w = v > w ? v : w;
             return w;
         };
+        std::vector<int> open;
         while (worst() >= o.tol && outer < o.max_outer) {
             outer++;
-            for (int r = 0; r < R; r++)
-                HZ_TRY(vec_scale(nm, nr[r] > 0 ? 1.0 / nr[r] : 0.0, R0 + r * nm, R1 + r * nm, Q0 + r * nm, Q1 + r * nm,
-                                 s));
+            open.clear();
+            for (int r = 0; r < R; r++) {
+                double *q0 = Q0 + r * nm, *q1 = Q1 + r * nm;
+                if (res[r] >= o.tol) {
+                    open.push_back(r);
+                    HZ_TRY(vec_scale(nm, 1.0 / nr[r], R0 + r * nm, R1 + r * nm, q0, q1, s));
+                } else {
+                    // a zero right-hand side: the column does not iterate
+                    HZ_CHECK_CUDA(cudaMemsetAsync(q0, 0, nm * sizeof(double), s));
+                    HZ_CHECK_CUDA(cudaMemsetAsync(q1, 0, nm * sizeof(double), s));
+                }
+            }
             int it = 0;
             std::vector<double> ires;
             HZ_TRY(b->multi.solve(A32, Q0, Q1, o.inner_tol, o.maxit, o.stagnation != 0, s, it, ires,
-                                  kInnerStallBatch));
+                                  kInnerStallBatch, &cit));
             iters += it;
-            pairs += 2LL * it * sq;
-            for (int r = 0; r < R; r++)
-                HZ_TRY(vec_axpy(nm, nr[r], b->multi.re(KrylovMulti::X) + r * nm, b->multi.im(KrylovMulti::X) + r * nm,
-                                X0 + r * nm, X1 + r * nm, s));
+            pairs += pairs_of(cit, 2);
+            A64.cols = open;
+            for (int r : open) {
+                const size_t off = (size_t)r * nm;
+                HZ_TRY(vec_axpy(nm, nr[r], b->multi.re(KrylovMulti::X) + off, b->multi.im(KrylovMulti::X) + off,
+                                X0 + off, X1 + off, s));
+            }
             HZ_TRY(A64.apply(R, X0, X1, Q0, Q1, s));
-            pairs += sq;
-            HZ_TRY(vec_sub((int64_t)tot, B0, B1, Q0, Q1, R0, R1, s));
-            for (int r = 0; r < R; r++) {
-                HZ_TRY(vec_norm(nm, R0 + r * nm, R1 + r * nm, part, dout, nr[r], s));
+            for (int r : open) {
+                const size_t off = (size_t)r * nm;
+                pairs += (long long)b->ops[r]->n * b->ops[r]->n;
+                HZ_TRY(vec_sub(nm, B0 + off, B1 + off, Q0 + off, Q1 + off, R0 + off, R1 + off, s));
+                HZ_TRY(vec_norm(nm, R0 + off, R1 + off, part, dout, nr[r], s));
                 res[r] = normb[r] > 0 ? nr[r] / normb[r] : 0.0;
             }
         }

@@ -198,15 +198,47 @@ struct DenseOp final : LinOp {
 };
 
 // Multi right-hand-side operator over the tube.
+// Columns that stopped iterating are left out of the sweep: the others are
+// packed into consecutive columns of `pack`, swept, and their products copied
+// back (the stopped columns' products are not read).  `pairs` counts the
+// kernel evaluations (one per pair for each group of multi_rhs_block()
+// columns).
 struct MultiMatrixFreeOp final : MultiOp {
     hz_operator *op;
     int precision;
-    DevBuf *scratch;
-    MultiMatrixFreeOp(hz_operator *o, int prec, DevBuf *sc) : op(o), precision(prec), scratch(sc) {}
+    DevBuf *scratch, *pack;
+    std::vector<int> cols;  // empty: every column
+    long long pairs = 0;
+    MultiMatrixFreeOp(hz_operator *o, int prec, DevBuf *sc, DevBuf *pk)
+        : op(o), precision(prec), scratch(sc), pack(pk) {}
     int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im, cudaStream_t s) override
     {
         HZ_TRY(scratch->ensure(multi_rhs_scratch_bytes(op->n, op->r32.npad)));
-        return sweep_multi(sweep_const(op), op->r32, rec64(op), precision, R, p_re, p_im, q_re, q_im, scratch->ptr, s);
+        const int64_t n = op->n;
+        const int m = cols.empty() ? R : (int)cols.size();
+        pairs += (long long)n * n * ((m + multi_rhs_block() - 1) / multi_rhs_block());
+        if (m == R)
+            return sweep_multi(sweep_const(op), op->r32, rec64(op), precision, R, p_re, p_im, q_re, q_im,
+                               scratch->ptr, s);
+        const size_t col = (size_t)n * sizeof(double), mn = (size_t)m * n;
+        HZ_TRY(pack->ensure(4 * mn * sizeof(double)));
+        double *pr = pack->as<double>(), *pi = pr + mn, *qr = pr + 2 * mn, *qi = pr + 3 * mn;
+        for (int j = 0; j < m; j++) {
+            HZ_CHECK_CUDA(cudaMemcpyAsync(pr + j * n, p_re + cols[j] * n, col, cudaMemcpyDeviceToDevice, s));
+            HZ_CHECK_CUDA(cudaMemcpyAsync(pi + j * n, p_im + cols[j] * n, col, cudaMemcpyDeviceToDevice, s));
+        }
+        HZ_TRY(sweep_multi(sweep_const(op), op->r32, rec64(op), precision, m, pr, pi, qr, qi, scratch->ptr, s));
+        for (int j = 0; j < m; j++) {
+            HZ_CHECK_CUDA(cudaMemcpyAsync(q_re + cols[j] * n, qr + j * n, col, cudaMemcpyDeviceToDevice, s));
+            HZ_CHECK_CUDA(cudaMemcpyAsync(q_im + cols[j] * n, qi + j * n, col, cudaMemcpyDeviceToDevice, s));
+        }
+        return HZ_OK;
+    }
+    int restrict_to(const std::vector<int> &c, cudaStream_t s) override
+    {
+        (void)s;
+        cols = c;
+        return HZ_OK;
     }
 };
 
@@ -253,7 +285,7 @@ struct hz_solver_state {
     KrylovMulti multi;
     DevBuf vec;  // b, x, r, q (re/im) for refinement
     DevBuf small;
-    DevBuf mvec, mscratch;  // multi right-hand side staging and sweep scratch
+    DevBuf mvec, mscratch, mpack;  // multi right-hand side staging, sweep scratch, packed columns
     DevBuf gwork, gsmall, gx;  // GMRES basis, Hessenberg partials, inner solution
 };
 
@@ -798,7 +830,7 @@ int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re
         dqi = b + 3 * tot;
     }
     HZ_CHECK_CUDA(cudaMemsetAsync(op->err.ptr, 0, sizeof(unsigned), s));
-    MultiMatrixFreeOp A(op, precision == HZ_PREC_F64 ? HZ_PREC_F64 : HZ_PREC_F32, &st->mscratch);
+    MultiMatrixFreeOp A(op, precision == HZ_PREC_F64 ? HZ_PREC_F64 : HZ_PREC_F32, &st->mscratch, &st->mpack);
     HZ_TRY(A.apply(nrhs, dpr, dpi, dqr, dqi, s));
     if (where == HZ_HOST) {
         HZ_TRY(stage_out(q_re, dqr, tot, where, s));
@@ -842,16 +874,17 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
     HZ_TRY(st->multi.reserve(n, nrhs));
     int iters = 0, outer = 0;
     long long pairs = 0;
-    const int blocks = (nrhs + multi_rhs_block() - 1) / multi_rhs_block();
     if (o.precision != HZ_PREC_F32_REFINED) {
-        MultiMatrixFreeOp A(op, o.precision, &st->mscratch);
+        MultiMatrixFreeOp A(op, o.precision, &st->mscratch, &st->mpack);
         HZ_TRY(st->multi.solve(A, B0, B1, o.tol, o.maxit, o.stagnation != 0, s, iters, res));
         HZ_CHECK_CUDA(cudaMemcpyAsync(X0, st->multi.re(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
         HZ_CHECK_CUDA(cudaMemcpyAsync(X1, st->multi.im(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        pairs = 2LL * iters * n * n * blocks;
+        pairs = A.pairs;
     } else {
-        // FP64 iterative refinement of every column: X += ||r_j|| A32^{-1} (r_j/||r_j||)
-        MultiMatrixFreeOp A32(op, HZ_PREC_F32, &st->mscratch), A64(op, HZ_PREC_F64, &st->mscratch);
+        // FP64 iterative refinement of every column still above tol:
+        // X += ||r_j|| A32^{-1} (r_j/||r_j||)
+        MultiMatrixFreeOp A32(op, HZ_PREC_F32, &st->mscratch, &st->mpack),
+            A64(op, HZ_PREC_F64, &st->mscratch, &st->mpack);
         HZ_TRY(st->small.ensure(vec_partial_bytes() + 64));
         double *part = st->small.as<double>();
         double *dout = part + (vec_partial_bytes() / sizeof(double));
@@ -868,26 +901,36 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
             for (double v : res) w = v > w ? v : w;
             return w;
         };
+        std::vector<int> open;
         while (worst() >= o.tol && outer < o.max_outer) {
             outer++;
-            for (int r = 0; r < nrhs; r++)
-                HZ_TRY(vec_scale(n, nr[r] > 0 ? 1.0 / nr[r] : 0.0, R0 + r * n, R1 + r * n, Q0 + r * n, Q1 + r * n, s));
+            open.clear();
+            for (int r = 0; r < nrhs; r++) {
+                if (res[r] >= o.tol) {
+                    open.push_back(r);
+                    HZ_TRY(vec_scale(n, 1.0 / nr[r], R0 + r * n, R1 + r * n, Q0 + r * n, Q1 + r * n, s));
+                } else {
+                    // a zero right-hand side: the column does not iterate
+                    HZ_CHECK_CUDA(cudaMemsetAsync(Q0 + r * n, 0, n * sizeof(double), s));
+                    HZ_CHECK_CUDA(cudaMemsetAsync(Q1 + r * n, 0, n * sizeof(double), s));
+                }
+            }
             int it = 0;
             std::vector<double> ires;
             HZ_TRY(st->multi.solve(A32, Q0, Q1, o.inner_tol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStall));
             iters += it;
-            pairs += 2LL * it * n * n * blocks;
-            for (int r = 0; r < nrhs; r++)
+            for (int r : open)
                 HZ_TRY(vec_axpy(n, nr[r], st->multi.re(KrylovMulti::X) + r * n, st->multi.im(KrylovMulti::X) + r * n,
                                 X0 + r * n, X1 + r * n, s));
+            HZ_TRY(A64.restrict_to(open, s));
             HZ_TRY(A64.apply(nrhs, X0, X1, Q0, Q1, s));
-            pairs += (long long)n * n * blocks;
-            HZ_TRY(vec_sub((int64_t)tot, B0, B1, Q0, Q1, R0, R1, s));
-            for (int r = 0; r < nrhs; r++) {
+            for (int r : open) {
+                HZ_TRY(vec_sub(n, B0 + r * n, B1 + r * n, Q0 + r * n, Q1 + r * n, R0 + r * n, R1 + r * n, s));
                 HZ_TRY(vec_norm(n, R0 + r * n, R1 + r * n, part, dout, nr[r], s));
                 res[r] = normb[r] > 0 ? nr[r] / normb[r] : 0.0;
             }
         }
+        pairs = A32.pairs + A64.pairs;
     }
     HZ_TRY(stage_out(x_re, X0, tot, where, s));
     HZ_TRY(stage_out(x_im, X1, tot, where, s));

@@ -210,8 +210,9 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
 double sweep32_reg_scale(int interior);
 // number of compiled FP32 sweep variants (block shape x targets per thread)
 int sweep32_num_configs();
-// Batched FP32 products (sweep_f32.cu): Q[r] = A_r P[r] for R operators in
-// one persistent launch; P, Q are [R][stride] column arrays.
+// Batched FP32 products (sweep_f32.cu): Q[r] = A_r P[r] for the described
+// operators of a batch in one persistent launch; P, Q are [ncols][stride]
+// column arrays and each described operator owns one column.
 struct Batch32Item {
     SweepConst c;
     Rec32 r;
@@ -219,12 +220,17 @@ struct Batch32Item {
     float4 *dens;
 };
 size_t batch32_desc_bytes(int R);
-int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, int64_t &units, int64_t &blocks,
-                     cudaStream_t s);
+// Describes nops operators: items[cols[i]] owning column cols[i] (cols NULL:
+// items[i], column i).
+int batch32_describe(const Batch32Item *items, int nops, int cfg, void *desc_dev, int64_t &units, int64_t &blocks,
+                     cudaStream_t s, const int *cols = nullptr);
 size_t batch32_partial_bytes();
-int sweep_f32_batch(int cfg, const void *desc_dev, int R, int64_t units, int64_t blocks, double4_32a *partial,
-                    size_t partial_bytes, const double *p_re, const double *p_im, double *q_re, double *q_im,
-                    int64_t stride, int64_t max_npad, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1);
+// Columns of described operators get their product; every column's padded
+// tail (and every column of an operator not described) is zeroed.
+int sweep_f32_batch(int cfg, const void *desc_dev, int nops, int ncols, int64_t units, int64_t blocks,
+                    double4_32a *partial, size_t partial_bytes, const double *p_re, const double *p_im,
+                    double *q_re, double *q_im, int64_t stride, int64_t max_npad, cudaStream_t s, cudaEvent_t ev0,
+                    cudaEvent_t ev1);
 // bytes of stream-K scratch that every FP32 sweep variant fits in
 size_t sweep32_partial_bytes();
 

@@ -81,7 +81,7 @@ __global__ void minit_kernel(int64_t n, const double *b_re, const double *b_im, 
     }
 }
 
-__global__ void mstart_kernel(int R, const double *partial, MScal *sc)
+__global__ void mstart_kernel(int R, const double *partial, MScal *sc, double *host)
 {
     const int r = threadIdx.x + blockIdx.x * blockDim.x;
     if (r >= R) return;
@@ -101,6 +101,8 @@ __global__ void mstart_kernel(int R, const double *partial, MScal *sc)
     c.best = 1e300;
     c.it = 0;
     c.best_it = 0;
+    host[2 * r] = c.err;
+    host[2 * r + 1] = c.active ? 1.0 : 0.0;
 }
 
 __global__ void mbeta_kernel(int R, const double *partial, MScal *sc)
@@ -283,7 +285,8 @@ int KrylovMulti::iteration(MultiOp &A, double tol, bool stagnation, int stall, c
 }
 
 int KrylovMulti::solve(MultiOp &A, const double *b_re, const double *b_im, double tol, int maxit, bool stagnation,
-                       cudaStream_t s, int &iters, std::vector<double> &resid, int stall)
+                       cudaStream_t s, int &iters, std::vector<double> &resid, int stall,
+                       std::vector<int> *col_iters)
 {
     double *pp = partial.as<double>();
     MScal *sc = scal.as<MScal>();
@@ -294,13 +297,25 @@ int KrylovMulti::solve(MultiOp &A, const double *b_re, const double *b_im, doubl
     HZ_CHECK_LAUNCH();
     mcdot_kernel<<<dim3(kMB, R), kMT, 0, s>>>(n, re(RV), im(RV), re(RV), im(RV), pp);
     HZ_CHECK_LAUNCH();
-    mstart_kernel<<<sb, 128, 0, s>>>(R, pp, sc);
+    mstart_kernel<<<sb, 128, 0, s>>>(R, pp, sc, host);
     HZ_CHECK_LAUNCH();
+    HZ_CHECK_CUDA(cudaStreamSynchronize(s));
     iters = 0;
     resid.assign(R, 0.0);
-    const uint64_t key = A.key();
+    if (col_iters) col_iters->assign(R, 0);
+    std::vector<int> cols;
+    auto active_cols = [&](std::vector<int> &out) {
+        out.clear();
+        for (int r = 0; r < R; r++)
+            if (host[2 * r + 1] > 0) out.push_back(r);
+    };
+    active_cols(cols);
+    if (cols.empty()) return HZ_OK;
+    HZ_TRY(A.restrict_to(cols, s));
+    std::vector<int> now;
     const int flags = (stagnation ? 1 : 0) | (stall << 1);
     for (int it = 1; it <= maxit; it++) {
+        const uint64_t key = A.key();
         if (key) {
             // one BiCGSTAB step per graph launch (captured on first use)
             if (!graph_exec || graph_key != key || graph_stream != s || graph_tol != tol || graph_flags != flags) {
@@ -338,12 +353,15 @@ int KrylovMulti::solve(MultiOp &A, const double *b_re, const double *b_im, doubl
         }
         HZ_CHECK_CUDA(cudaStreamSynchronize(s));
         iters = it;
-        int active = 0;
-        for (int r = 0; r < R; r++) {
-            resid[r] = host[2 * r];
-            if (host[2 * r + 1] > 0) active++;
+        for (int r = 0; r < R; r++) resid[r] = host[2 * r];
+        if (col_iters)
+            for (int r : cols) (*col_iters)[r]++;
+        active_cols(now);
+        if (now.empty()) break;
+        if (now.size() != cols.size()) {
+            cols.swap(now);
+            HZ_TRY(A.restrict_to(cols, s));
         }
-        if (!active) break;
     }
     return HZ_OK;
 }

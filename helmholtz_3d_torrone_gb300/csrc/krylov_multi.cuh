@@ -16,6 +16,16 @@ struct MultiOp {
     // synchronisation), so a solver iteration around it can be captured in a
     // CUDA graph; the value identifies the operator the graph was built for
     virtual uint64_t key() const { return 0; }
+    // The solver calls this with the columns still iterating, before its
+    // first iteration and whenever a column stops: an operator may then skip
+    // the others (their products are not read).  A change of what apply
+    // enqueues must change key().
+    virtual int restrict_to(const std::vector<int> &cols, cudaStream_t s)
+    {
+        (void)cols;
+        (void)s;
+        return HZ_OK;
+    }
 };
 
 class KrylovMulti {
@@ -24,8 +34,10 @@ class KrylovMulti {
     ~KrylovMulti();
     int reserve(int64_t n, int R);
     // Solve A X = B column by column (x0 = 0); B on the device, [R][n].
+    // col_iters (optional): the iterations each column took part in.
     int solve(MultiOp &A, const double *b_re, const double *b_im, double tol, int maxit, bool stagnation,
-              cudaStream_t s, int &iters, std::vector<double> &resid, int stall = 0);
+              cudaStream_t s, int &iters, std::vector<double> &resid, int stall = 0,
+              std::vector<int> *col_iters = nullptr);
     double *re(int v);
     double *im(int v);
 

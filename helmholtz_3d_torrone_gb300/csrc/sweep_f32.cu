@@ -344,6 +344,7 @@ struct BatchOp {
     int64_t block0;  // first global target block
     int64_t blocks, ntiles;
     int dir;
+    int col;         // column of P and Q
     double scale;    // sg / (4 pi), folded into the densities
 };
 
@@ -357,7 +358,7 @@ struct BatchVec {
 __global__ void batch_prep_kernel(const BatchOp *__restrict__ ops, BatchVec v)
 {
     const BatchOp &o = ops[blockIdx.y];
-    const double *pr = v.p_re + blockIdx.y * v.stride, *pi = v.p_im + blockIdx.y * v.stride;
+    const double *pr = v.p_re + (int64_t)o.col * v.stride, *pi = v.p_im + (int64_t)o.col * v.stride;
     float4 *dens = const_cast<float4 *>(o.a.dens);
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < o.a.npad;
          s += (int64_t)gridDim.x * blockDim.x) {
@@ -522,8 +523,9 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_batch_kernel(const BatchOp *
                             : batch_tiles<false, NT, TG>(a, ops, nops, o, u, seg_end, u_begin, u_end, blk, slot0, th,
                                                          tl, tn, treg, hAr, lAr, hAi, lAi, sp, sn, sd, bar);
         if (!ok) return;
-        const double *pr = v.p_re + o * v.stride, *pi = v.p_im + o * v.stride;
-        double *qr = v.q_re + o * v.stride, *qi = v.q_im + o * v.stride;
+        const int64_t off = (int64_t)ops[o].col * v.stride;
+        const double *pr = v.p_re + off, *pi = v.p_im + off;
+        double *qr = v.q_re + off, *qi = v.q_im + off;
 #pragma unroll
         for (int g = 0; g < TG; g++) {
             const double ar = (double)hAr[g] + (double)lAr[g], ai = (double)hAi[g] + (double)lAi[g];
@@ -561,8 +563,8 @@ __global__ void __launch_bounds__(256) sweep32_batch_fixup(const BatchOp *__rest
             ar += q.x;
             ai += q.y;
         }
-        batch_write(a, blk * SLOTS + k, ar, ai, v.p_re + o * v.stride, v.p_im + o * v.stride, v.q_re + o * v.stride,
-                    v.q_im + o * v.stride);
+        const int64_t off = (int64_t)ops[o].col * v.stride;
+        batch_write(a, blk * SLOTS + k, ar, ai, v.p_re + off, v.p_im + off, v.q_re + off, v.q_im + off);
     }
 }
 
@@ -721,7 +723,7 @@ size_t sweep32_partial_bytes()
 size_t batch32_desc_bytes(int R) { return (size_t)R * sizeof(BatchOp); }
 
 int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, int64_t &units, int64_t &blocks,
-                     cudaStream_t s)
+                     cudaStream_t s, const int *cols)
 {
     static const int kSlots[kShapes] = {512, 256, 256, 256};  // NT * TG of shapes 0..3 (launch_cfg)
     const int slots = kSlots[cfg % kShapes];
@@ -729,9 +731,11 @@ int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, i
     units = 0;
     blocks = 0;
     for (int r = 0; r < R; r++) {
-        const Batch32Item &it = items[r];
+        const int col = cols ? cols[r] : r;
+        const Batch32Item &it = items[col];
         BatchOp &b = h[r];
         memset(&b, 0, sizeof(b));
+        b.col = col;
         Args32 &a = b.a;
         a.n = it.c.n;
         a.npad = it.r.npad;
@@ -755,7 +759,7 @@ int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, i
         a.pos64 = it.pos64;
         a.err = it.c.err;
         if (it.r.npad % slots != 0) {
-            set_error("batched FP32 sweep: operator %d has %lld slots, not a multiple of %d", r,
+            set_error("batched FP32 sweep: operator %d has %lld slots, not a multiple of %d", col,
                       (long long)it.r.npad, slots);
             return HZ_ERR_STATE;
         }
@@ -785,16 +789,17 @@ size_t batch32_partial_bytes()
     return m;
 }
 
-int sweep_f32_batch(int cfg, const void *desc_dev, int R, int64_t units, int64_t blocks, double4_32a *partial,
-                    size_t partial_bytes, const double *p_re, const double *p_im, double *q_re, double *q_im,
-                    int64_t stride, int64_t max_npad, cudaStream_t s, cudaEvent_t ev0, cudaEvent_t ev1)
+int sweep_f32_batch(int cfg, const void *desc_dev, int R, int ncols, int64_t units, int64_t blocks,
+                    double4_32a *partial, size_t partial_bytes, const double *p_re, const double *p_im,
+                    double *q_re, double *q_im, int64_t stride, int64_t max_npad, cudaStream_t s, cudaEvent_t ev0,
+                    cudaEvent_t ev1)
 {
+    // padded tails of the columns stay zero
+    HZ_CHECK_CUDA(cudaMemsetAsync(q_re, 0, (size_t)ncols * stride * sizeof(double), s));
+    HZ_CHECK_CUDA(cudaMemsetAsync(q_im, 0, (size_t)ncols * stride * sizeof(double), s));
     if (R <= 0 || units <= 0) return HZ_OK;
     const BatchOp *ops = static_cast<const BatchOp *>(desc_dev);
     BatchVec v{p_re, p_im, q_re, q_im, stride};
-    // padded tails of the columns stay zero
-    HZ_CHECK_CUDA(cudaMemsetAsync(q_re, 0, (size_t)R * stride * sizeof(double), s));
-    HZ_CHECK_CUDA(cudaMemsetAsync(q_im, 0, (size_t)R * stride * sizeof(double), s));
     long long bx = (max_npad + 255) / 256;
     if (bx > 256) bx = 256;
     batch_prep_kernel<<<dim3((unsigned)bx, (unsigned)R), 256, 0, s>>>(ops, v);

@@ -64,3 +64,26 @@ def test_batch_refined_solve(hz, batch):
     for op, rhs, x in zip(ops, bs, xs):
         x64, i64 = op.solve(rhs, method=hz.BICGSTAB, precision=hz.PREC_F64, tol=1e-12)
         assert rel_err(x, x64) < 1e-8
+
+
+@pytest.mark.parametrize("precision", ["f64", "refined"])
+def test_batch_columns_leave_when_converged(hz, batch, precision):
+    """A zero right-hand side never iterates and the others stop at their own
+    iteration counts: the launch is re-described over the columns still
+    iterating, so the pairs evaluated are fewer than lockstep would take,
+    and every system still equals its own FP64 solve."""
+    b, ops = batch
+    bs = [op.rhs_point_source(np.array([0.05, 0.02, 0.01]), hz.RHS_POINT_DIRICHLET) for op in ops]
+    bs[1] = np.zeros_like(bs[1])
+    prec = hz.PREC_F64 if precision == "f64" else hz.PREC_F32_REFINED
+    xs, info, res = b.solve(bs, precision=prec, tol=1e-11, inner_tol=1e-5, maxit=400)
+    assert np.all(res < 1e-11)
+    assert not np.any(xs[1])
+    sq = sum(op.n * op.n for i, op in enumerate(ops) if i != 1)
+    lockstep = 2 * info["iterations"] * sq + info["outer"] * sq
+    assert info["pair_evals"] < lockstep
+    for i, (op, rhs, x) in enumerate(zip(ops, bs, xs)):
+        if i == 1:
+            continue
+        x64, _ = op.solve(rhs, method=hz.BICGSTAB, precision=hz.PREC_F64, tol=1e-12)
+        assert rel_err(x, x64) < 1e-8

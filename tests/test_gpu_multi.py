@@ -62,3 +62,24 @@ def test_batched_solve_matches_single(hz, torus_op, precision):
     for r in [0, 4, 9]:
         x, _ = op.solve(B[r], method=hz.BICGSTAB, precision=hz.PREC_F64, tol=1e-9)
         assert rel_err(X[r], x) < 1e-7
+
+
+@pytest.mark.parametrize("precision", ["f64", "refined"])
+def test_multi_columns_leave_when_converged(hz, torus_op, precision):
+    """A zero column and columns of different difficulty (plane waves and a
+    point source): stopped columns leave the packed sweep, the others still
+    equal their single solves, and the zero column stays zero."""
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    op = torus_op
+    B = op.rhs_plane_waves(G.fibonacci_sphere(10))
+    B[3] = 0.0
+    B[7] = op.rhs_point_source(np.array([0.5, 0.0, 0.0]), hz.RHS_POINT_DIRICHLET)
+    prec = hz.PREC_F64 if precision == "f64" else hz.PREC_F32_REFINED
+    X, info, res = op.solve_multi(B, method=hz.BICGSTAB, precision=prec, tol=1e-9, inner_tol=1e-5)
+    assert np.all(res < 1e-9)
+    assert not np.any(X[3])
+    blocks = 2  # 10 columns in groups of 8
+    assert info["pair_evals"] <= (2 * info["iterations"] + info["outer"]) * op.n * op.n * blocks
+    for r in [0, 7, 9]:
+        x, _ = op.solve(B[r], method=hz.BICGSTAB, precision=hz.PREC_F64, tol=1e-9)
+        assert rel_err(X[r], x) < 1e-7
