@@ -73,6 +73,13 @@ def parse():
                     help="--solve: torus (the step workload) or the ellipsoid (0.7,0.5,0.4) level set "
                          "reinitialised on the device before the build")
     ap.add_argument("--reinit-iters", type=int, default=60, help="--solve --shape ellipsoid: TVD-RK2 steps")
+    ap.add_argument("--combo", action="store_true",
+                    help="instead of the step benchmark: the Combo formulation (sphere r = 1 in [-2,2]^3, annulus "
+                         "[0.1 sqrt(h), sqrt(h)], exterior monopole Neumann data): FP64 and FP32 product rates, a "
+                         "refined solve, and with --fp64-full the FP64 solve")
+    ap.add_argument("--gradient", action="store_true",
+                    help="instead of the step benchmark: misfit gradients on the bumpy sphere (dJ/dphi at every "
+                         "grid node, dJ/dg, dJ/dk by adjoint solves) with central-difference checks")
     ap.add_argument("--plane-waves", type=int, default=0,
                     help="instead of the step benchmark: solve this many incident plane waves (Fibonacci-sphere "
                          "directions) on the torus with the multi right-hand-side solver and report the times")
@@ -466,6 +473,162 @@ def run_plane_waves(a):
     return 0
 
 
+def run_combo(a):
+    """The Combo formulation at scale: FP64 and FP32 matrix-free products,
+    an FP32 + FP64-refinement solve and (with --fp64-full) the plain FP64
+    solve, and the field at (1.5, 0.3, 0.2) against the exact exterior
+    monopole -e^{ikr}/(kr)."""
+    import numpy as np
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    N, k, tol = a.N, a.wave, min(a.tol)
+    H = 4.0 / N
+    eps0 = np.sqrt(H)
+    p = hz.params(N, k)  # [-2,2]^3, FACTOR 2, Neumann, exterior (the reference's defaults)
+    o = hz.dense_opts(hz.DENSE_COMBO, p, delta0=0.1 * eps0, epsilon=eps0, wavenum=k, eta=-1.0)
+    d = G.sphere(N, radius=1.0, center=(0.013, 0.021, 0.007), int_l=-2.0, int_u=2.0)
+    out = {"mode": "combo"}
+    t0 = time.perf_counter()
+    with hz.Operator(p) as op:
+        op.set_combo(o)
+        op.set_distance(d)
+        n = op.build()
+        out["config"] = {"workload": "Combo formulation: sphere r = 1 centred near the origin on %d^3 over "
+                                     "[-2,2]^3, annulus 0.1 sqrt(h) <= |d| <= sqrt(h), SineWeight, eta = -1, "
+                                     "k = %g, exterior monopole Neumann data" % (N, k),
+                         "N": N, "n_annulus": n, "wave": k, "build_s": time.perf_counter() - t0}
+        rng = np.random.default_rng(1)
+        v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        prod = {}
+        for name, prec, reps in (("f32", hz.PREC_F32, 5), ("f64", hz.PREC_F64, 1)):
+            op.matvec(v, precision=prec)
+            t1 = time.perf_counter()
+            for _ in range(reps):
+                q = op.matvec(v, precision=prec)
+            dt = (time.perf_counter() - t1) / reps
+            prod[name] = {"seconds": dt, "gpair_per_s": float(n) * n / dt / 1e9}
+            prod[name + "_q"] = q
+        prod["f32_rel_err_vs_f64"] = float(np.linalg.norm(prod.pop("f32_q") - prod["f64_q"]) /
+                                           np.linalg.norm(prod.pop("f64_q")))
+        out["products"] = dict(prod, note="wall time of hz_matvec incl. host<->device copies")
+        b = op.rhs_point_source(np.zeros(3), hz.RHS_MONOPOLE_NEUMANN)
+        rx = np.array([[1.5, 0.3, 0.2]])
+        r = float(np.linalg.norm(rx))
+        ue = -np.exp(1j * k * r) / (k * r)
+        x, info = op.solve(b, method=hz.GMRES, precision=hz.PREC_F32_REFINED, tol=tol, inner_tol=1e-5,
+                           maxit=3000, restart=a.restart)
+        u = op.evaluate(rx, x, hz.COMBO_LAYER)[0]
+        out["refined_solve"] = dict(info, method="gmres(%d)" % a.restart, tol=tol,
+                                    field_rel_err_vs_exact=float(abs(u - ue) / abs(ue)))
+        if a.fp64_full:
+            x64, i64 = op.solve(b, method=hz.GMRES, precision=hz.PREC_F64, tol=tol, maxit=3000, restart=a.restart)
+            u64 = op.evaluate(rx, x64, hz.COMBO_LAYER)[0]
+            out["f64_solve"] = dict(i64, method="gmres(%d)" % a.restart, tol=tol,
+                                    field_rel_err_vs_exact=float(abs(u64 - ue) / abs(ue)))
+            out["density_rel_err_refined_vs_f64"] = float(np.max(np.abs(x - x64)) / np.max(np.abs(x64)))
+            out["speedup_refined_vs_f64"] = i64["seconds"] / info["seconds"]
+    print(json.dumps(out))
+    sys.stdout.flush()
+    return 0
+
+
+def run_gradient(a):
+    """Misfit gradients by adjoint solves on the bumpy sphere
+    r = 0.5 (1 + 0.08 cos 3theta sin 2phi), its level set reinitialised on the
+    device: J = sum |u(x_m) - t_m|^2 over 64 receivers on r = 0.95, t the
+    field of the unperturbed sphere on the same grid.  dJ/dphi at every grid
+    node (hz_shape_gradient) and dJ/dg, dJ/dk (hz_misfit_gradient) are timed
+    and checked against central differences (step 1e-6) of complete refined
+    solves (FP32 sweeps, FP64 residuals, to --tol)."""
+    import numpy as np
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    N, wave, tol = a.N, a.wave, min(a.tol)
+    H = 2.0 / N
+    eps = 3.0 * H
+    src = np.array([0.05, 0.02, 0.01])
+    rx = G.random_sphere_points(64, 0.95, seed=17)
+    sk = dict(method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=tol, inner_tol=1e-5, maxit=3000)
+    step = 1e-6
+
+    def params(k):
+        return hz.params(N, k, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1)
+
+    def field(dist, k=wave, b=None):
+        with hz.Operator(params(k)) as op:
+            op.set_distance(dist)
+            op.build()
+            if b is None:
+                b = op.rhs_point_source(src, hz.RHS_POINT_DIRICHLET)
+            x, info = op.solve(b, **sk)
+            return op.evaluate(rx, x, hz.DOUBLE_LAYER), info
+
+    t0 = time.perf_counter()
+    d = hz.reinitialize(G.bumpy_sphere_levelset(N), N, H, a.reinit_iters)
+    target, _ = field(G.sphere(N, 0.5))
+    setup_s = time.perf_counter() - t0
+
+    def J_of(dist, k=wave, b=None):
+        u, _ = field(dist, k, b)
+        return float(np.sum(np.abs(u - target) ** 2))
+
+    out = {"mode": "gradient", "config": {
+        "workload": "bumpy sphere r = 0.5(1 + 0.08 cos3theta sin2phi), level set reinitialised by %d TVD-RK2 steps "
+                    "on %d^3 over [-1,1]^3, tube |phi|<=3h, k=%g, Dirichlet point source at (0.05,0.02,0.01); "
+                    "J = sum |u - t|^2 at 64 seeded receivers on r = 0.95, t from the sphere r = 0.5 on the same grid"
+                    % (a.reinit_iters, N, wave),
+        "N": N, "wave": wave, "tol": tol, "fd_step": step, "setup_s": setup_s}}
+    with hz.Operator(params(wave)) as op:
+        op.set_distance(d)
+        n = op.build()
+        out["config"]["n_tube"] = n
+        op.autotune()
+        b = op.rhs_point_source(src, hz.RHS_POINT_DIRICHLET)
+        J, gphi, info = op.shape_gradient(src, rx, target, **sk)
+        out["shape_gradient"] = dict(info, J=J)
+        J2, gb, dk, gw, info2 = op.misfit_gradient(b, rx, target, **sk)
+        out["misfit_gradient"] = dict(info2, J=J2, dJ_dk=dk)
+    t0 = time.perf_counter()
+    checks = []
+    rng = np.random.default_rng(5)
+    inner = np.argwhere(np.abs(d) < eps - 0.5 * H)
+
+    def fd_phi(q, h):
+        dp, dm = d.copy(), d.copy()
+        dp[q] += h
+        dm[q] -= h
+        return (J_of(dp) - J_of(dm)) / (2 * h)
+
+    for q in (tuple(int(v) for v in inner[i]) for i in rng.choice(len(inner), 8, replace=False)):
+        fd, fd7 = fd_phi(q, step), fd_phi(q, 0.1 * step)
+        # a jump of J inside [phi - h, phi + h] shows as quotients that
+        # disagree between the two steps
+        checks.append({"wrt": "phi%s" % (q,), "phi": float(d[q]), "adjoint": float(gphi[q]), "fd": fd,
+                       "fd_step_1e-7": fd7, "smooth": bool(abs(fd - fd7) <= 1e-2 * abs(fd7))})
+    fdk = (J_of(d, wave + step, b) - J_of(d, wave - step, b)) / (2 * step)
+    checks.append({"wrt": "k", "adjoint": dk, "fd": fdk})
+    for i in (int(rng.integers(n)),):
+        for part, unit in (("re", 1.0), ("im", 1j)):
+            e = np.zeros(n, dtype=complex)
+            e[i] = unit * step
+            fd = (J_of(d, wave, b + e) - J_of(d, wave, b - e)) / (2 * step)
+            adj = gb[i].real if part == "re" else gb[i].imag
+            checks.append({"wrt": "%s g[%d]" % (part, i), "adjoint": float(adj), "fd": fd})
+    for c in checks:
+        c["rel_diff"] = abs(c["adjoint"] - c["fd"]) / max(abs(c["fd"]), 1e-300)
+    out["fd_checks"] = checks
+    sm = [c for c in checks if c.get("smooth")]
+    out["phi_nodes_smooth"] = "%d of %d" % (len(sm), sum(1 for c in checks if "smooth" in c))
+    if sm:
+        out["phi_max_rel_diff_smooth"] = max(c["rel_diff"] for c in sm)
+    out["fd_seconds"] = time.perf_counter() - t0
+    out["note"] = ("J is piecewise smooth in phi: a node whose step moves a pair across the near-field radius or "
+                   "flips an upwind branch of the stencils shows the jump in its difference quotient")
+    print(json.dumps(out))
+    sys.stdout.flush()
+    return 0
+
+
 def run_batch(a):
     """An uneven batch of ellipsoids solved together (hz_batch_solve: one
     persistent FP32 launch per product over all surfaces) against the same
@@ -529,9 +692,13 @@ def main():
     rank, world, local = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
-    if a.solve or a.plane_waves or a.batch:
+    if a.solve or a.plane_waves or a.batch or a.gradient or a.combo:
         import torch
         torch.cuda.set_device(local)
+        if a.gradient:
+            return run_gradient(a)
+        if a.combo:
+            return run_combo(a)
         if a.plane_waves:
             return run_plane_waves(a)
         if a.batch:

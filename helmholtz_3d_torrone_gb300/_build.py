@@ -26,6 +26,7 @@ UNITS = {
     "sweep_f64.cu": [],
     "sweep_f32.cu": ["-ftz=true"],
     "sweep_multi.cu": ["-ftz=true"],
+    "sweep_combo32.cu": ["-ftz=true"],
     "krylov_multi.cu": [],
     "krylov.cu": [],
     "gmres.cu": [],

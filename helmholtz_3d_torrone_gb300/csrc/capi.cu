@@ -129,10 +129,10 @@ struct MatrixFreeOp final : LinOp {
         cudaEvent_t e0 = slot >= 0 ? op->timer.start[slot] : nullptr;
         cudaEvent_t e1 = slot >= 0 ? op->timer.stop[slot] : nullptr;
         if (op->combo) {
-            if (precision != HZ_PREC_F64) {
-                set_error("the Combo formulation has FP64 products only");
-                return HZ_ERR_ARG;
-            }
+            if (precision != HZ_PREC_F64)
+                return sweep_combo32(c, op->r32, op->pos64.as<double4_32a>(), op->combo_opts.wavenum,
+                                     op->combo_opts.eta, mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im,
+                                     op->dens32.as<float4>(), s, e0, e1);
             return sweep_combo64(op->n, op->p.wave, op->combo_opts.wavenum, op->combo_opts.eta, op->tau,
                                  op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->adist.as<double>(),
                                  mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im, s, e0, e1);
@@ -333,6 +333,54 @@ int need_built(hz_operator *op)
 
 }  // namespace
 
+// FP32 sweep records of the tube (or annulus) points in blocked order.
+static int build_records32(hz_operator *op, double reg_scale)
+{
+    cudaStream_t s = op->stream;
+    const int N = op->p.N;
+    const int64_t n = op->n;
+    const int64_t unit = (int64_t)kThreads32 * kTgt32;  // multiple of kTile32
+    const int64_t npad = ((n + unit - 1) / unit) * unit;
+    op->r32.npad = npad;
+    if (npad > 0) {
+        HZ_TRY(op->perm.ensure(npad * sizeof(int)));
+        HZ_TRY(op->pos32.ensure(npad * sizeof(float4)));
+        HZ_TRY(op->nrm32.ensure(npad * sizeof(float4)));
+        HZ_TRY(op->tpos32.ensure(npad * sizeof(double4_32a)));
+        const int64_t ntiles = npad / kTile32;
+        op->r32.mwords = (ntiles + 31) / 32;
+        HZ_TRY(op->origin32.ensure(ntiles * sizeof(double4_32a)));
+        HZ_TRY(op->split32.ensure((2 * npad + 2 * ntiles) * sizeof(float4)));
+        HZ_TRY(op->nearmask32.ensure(ntiles * op->r32.mwords * sizeof(uint32_t)));
+        HZ_TRY(op->dens32.ensure(npad * sizeof(float4)));
+        HZ_TRY(sweep_order(N, n, op->idx.as<int64_t>(), op->perm.as<int>(), npad, op->scratch, s));
+    }
+    op->r32.perm = op->perm.as<int>();
+    op->r32.pos = op->pos32.as<float4>();
+    op->r32.nrm = op->nrm32.as<float4>();
+    op->r32.origin = op->origin32.as<double4_32a>();
+    op->r32.tpos = op->tpos32.as<double4_32a>();
+    {
+        float4 *sp = op->split32.as<float4>();
+        const int64_t ntiles = npad / kTile32;
+        op->r32.thi = sp;
+        op->r32.tlo = sp ? sp + npad : nullptr;
+        op->r32.ohi = sp ? sp + 2 * npad : nullptr;
+        op->r32.olo = sp ? sp + 2 * npad + ntiles : nullptr;
+        op->r32.nearmask = op->nearmask32.as<uint32_t>();
+    }
+    if (npad > 0) {
+        const size_t pb = sweep32_partial_bytes();
+        HZ_TRY(op->partial32.ensure(pb));
+        op->r32.partial = op->partial32.as<double4_32a>();
+        op->r32.partial_bytes = pb;
+    }
+    if (npad > 0)
+        HZ_TRY(build_rec32(op->r32, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
+                           reg_scale, op->tau, s));
+    return HZ_OK;
+}
+
 // hz_build for the Combo formulation: annulus selection and per-point rows
 // of new_HelmholtzKernelCombo (dense.cu), packed into the operator's arrays.
 static int build_combo(hz_operator *op, int64_t *n_out)
@@ -355,7 +403,10 @@ static int build_combo(hz_operator *op, int64_t *n_out)
                       op->adist.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), s));
     HZ_CHECK_CUDA(cudaMemsetAsync(op->dreg.ptr, 0, nn * sizeof(double), s));
     HZ_TRY(check_device_error(op, "hz_build (Combo)"));
-    op->r32.npad = 0;  // no FP32 records: FP64 products only
+    // FP32 records as the classic operator's (reg scaled by 4 pi: the Combo
+    // kernel's c4 = 1/(4 pi) is folded into the densities), |d| in nrm32.w
+    HZ_TRY(build_records32(op, 4.0 * 3.14159265358979323846264338328));
+    HZ_TRY(combo32_set_distances(op->r32, op->adist.as<double>(), s));
     HZ_TRY(op->scratch.ensure(nn * sizeof(double4_32a) + 256));
     HZ_TRY(op->io.ensure(nn * sizeof(double) * 8));
     HZ_CHECK_CUDA(cudaStreamSynchronize(s));
@@ -544,46 +595,7 @@ int hz_build(hz_operator *op, int64_t *n_out)
                      op->w.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->err.as<unsigned>(), s,
                      op->dreg.as<double>()));
     HZ_TRY(check_device_error(op, "hz_build"));
-    // FP32 sweep records in blocked order
-    const int64_t unit = (int64_t)kThreads32 * kTgt32;  // multiple of kTile32
-    const int64_t npad = ((n + unit - 1) / unit) * unit;
-    op->r32.npad = npad;
-    if (npad > 0) {
-        HZ_TRY(op->perm.ensure(npad * sizeof(int)));
-        HZ_TRY(op->pos32.ensure(npad * sizeof(float4)));
-        HZ_TRY(op->nrm32.ensure(npad * sizeof(float4)));
-        HZ_TRY(op->tpos32.ensure(npad * sizeof(double4_32a)));
-        const int64_t ntiles = npad / kTile32;
-        op->r32.mwords = (ntiles + 31) / 32;
-        HZ_TRY(op->origin32.ensure(ntiles * sizeof(double4_32a)));
-        HZ_TRY(op->split32.ensure((2 * npad + 2 * ntiles) * sizeof(float4)));
-        HZ_TRY(op->nearmask32.ensure(ntiles * op->r32.mwords * sizeof(uint32_t)));
-        HZ_TRY(op->dens32.ensure(npad * sizeof(float4)));
-        HZ_TRY(sweep_order(N, n, op->idx.as<int64_t>(), op->perm.as<int>(), npad, op->scratch, s));
-    }
-    op->r32.perm = op->perm.as<int>();
-    op->r32.pos = op->pos32.as<float4>();
-    op->r32.nrm = op->nrm32.as<float4>();
-    op->r32.origin = op->origin32.as<double4_32a>();
-    op->r32.tpos = op->tpos32.as<double4_32a>();
-    {
-        float4 *sp = op->split32.as<float4>();
-        const int64_t ntiles = npad / kTile32;
-        op->r32.thi = sp;
-        op->r32.tlo = sp ? sp + npad : nullptr;
-        op->r32.ohi = sp ? sp + 2 * npad : nullptr;
-        op->r32.olo = sp ? sp + 2 * npad + ntiles : nullptr;
-        op->r32.nearmask = op->nearmask32.as<uint32_t>();
-    }
-    if (npad > 0) {
-        const size_t pb = sweep32_partial_bytes();
-        HZ_TRY(op->partial32.ensure(pb));
-        op->r32.partial = op->partial32.as<double4_32a>();
-        op->r32.partial_bytes = pb;
-    }
-    if (npad > 0)
-        HZ_TRY(build_rec32(op->r32, op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(),
-                           sweep32_reg_scale(op->p.interior), op->tau, s));
+    HZ_TRY(build_records32(op, sweep32_reg_scale(op->p.interior)));
     // scratch for the FP64 sweep densities (double4_32a per point) and staging
     HZ_TRY(op->scratch.ensure(nn * sizeof(double4_32a) + 256));
     HZ_TRY(op->io.ensure(nn * sizeof(double) * 8));
@@ -1118,10 +1130,6 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
     if (opts_in) o = *opts_in;
     else hz_solve_opts_default(&o);
     HZ_TRY(check_opts(o));
-    if (op->combo && o.precision != HZ_PREC_F64) {
-        set_error("hz_solve: the Combo formulation solves in FP64 only");
-        return HZ_ERR_ARG;
-    }
     HZ_CHECK_CUDA(cudaSetDevice(op->device));
     cudaStream_t s = op->stream;
     const int64_t n = op->n;

@@ -12,10 +12,13 @@
 //                    offset point x*_i + |d_j| n_i and x*_j.
 // A p:    q_i  = sum_j kappa_ij (r_j p_j) + (i eta / 2) p_i,
 // A^H pt: qt_j = r_j sum_i conj(kappa_ij) pt_i - (i eta / 2) pt_j.
-// Every entry is recomputed per product (two square roots, two sin/cos
-// pairs), so the sweep is bound by the FP64 pipe; sources are staged in
-// shared memory tile by tile.
+// Every entry is recomputed per product, so the sweep is bound by the FP64
+// pipe: 1/r and 1/|y| come from rsqrt, both sin/cos pairs from the table
+// method of sincos64.cuh, and the near-field test sqrt(r^2) > tau is
+// evaluated exactly only where r^2 lies within a relative 1e-12 of tau^2.
+// Sources are staged in shared memory tile by tile.
 #include "hz_internal.cuh"
+#include "sincos64.cuh"
 
 namespace hz {
 namespace {
@@ -26,7 +29,7 @@ constexpr int kComboTile = 128;
 
 struct ComboArgs {
     int64_t n;
-    double wave, wavenum, eta, tau;
+    double wave, wavenum, eta, tau, tau2;
     const double4_32a *pos;  // (x*, reg)
     const double4_32a *nrm;  // (n, r)
     const double *adist;     // |d|
@@ -37,19 +40,23 @@ struct ComboArgs {
 // kappa_ij of the header: target point i (x*_i, n_i, reg_i) and source
 // point j (x*_j, n_j, |d_j|), in the reference's term order
 // (HelmholtzKernel.c:441-576).
-__device__ __forceinline__ void combo_kappa(const ComboArgs &a, double xi, double yi, double zi, double nxi,
-                                            double nyi, double nzi, double regi, double xj, double yj, double zj,
-                                            double nxj, double nyj, double nzj, double dj, double &kr, double &ki)
+__device__ __forceinline__ void combo_kappa(const ComboArgs &a, const double2 *tab, double xi, double yi, double zi,
+                                            double nxi, double nyi, double nzi, double regi, double xj, double yj,
+                                            double zj, double nxj, double nyj, double nzj, double dj, double &kr,
+                                            double &ki)
 {
     const double W = a.wave, k = a.wavenum;
     const double c4 = 1. / (4. * kPi);
     const double m1 = xi - xj, m2 = yi - yj, m3 = zi - zj;
-    const double mn = sqrt(m1 * m1 + m2 * m2 + m3 * m3);
+    const double r2 = m1 * m1 + m2 * m2 + m3 * m3;
+    bool far = r2 > a.tau2;
+    if (fabs(r2 - a.tau2) <= 1e-12 * a.tau2) far = sqrt(r2) > a.tau;
     double part, parti;
-    if (mn > a.tau) {
-        const double rn = 1. / mn;
+    if (far) {
+        const double rn = rsqrt(r2);
+        const double mn = r2 * rn;
         double sv, cv;
-        sincos(W * mn, &sv, &cv);
+        table_sincos(W * mn, tab, sv, cv);
         const double es = sv * rn, ec = cv * rn;
         const double den = c4 * rn * rn;
         const double c1 = -1. * (W * sv + ec) * den;
@@ -62,15 +69,16 @@ __device__ __forceinline__ void combo_kappa(const ComboArgs &a, double xi, doubl
         parti = 0.0;
     }
     const double y1 = xi + dj * nxi - xj, y2 = yi + dj * nyi - yj, y3 = zi + dj * nzi - zj;
-    const double yn = sqrt(y1 * y1 + y2 * y2 + y3 * y3);
-    const double rn = 1. / yn;
+    const double ysq = y1 * y1 + y2 * y2 + y3 * y3;
+    const double rn = rsqrt(ysq);
+    const double yn = ysq * rn;
     const double ip1 = nxi * nxj + nyi * nyj + nzi * nzj;
     const double ip2 = y1 * nxi + y2 * nyi + y3 * nzi;
     const double ip3 = y1 * nxj + y2 * nyj + y3 * nzj;
     const double cm1 = ip1 * rn;
     const double cm2 = ip2 * rn * ip3 * rn;
     double s0, c0;
-    sincos(k * yn, &s0, &c0);
+    table_sincos(k * yn, tab, s0, c0);
     const double cv = c0 * rn, sv = s0 * rn;
     const double t1r = -1. * (cv * rn + k * sv) * cm1;
     const double t1i = (k * cv - sv * rn) * cm1;
@@ -93,6 +101,8 @@ __global__ void __launch_bounds__(kComboThreads) combo_sweep_kernel(ComboArgs a)
     __shared__ double4_32a sp[kComboTile], sn[kComboTile];
     __shared__ double2 sd[kComboTile];  // ADJ: pt_i; else r_j p_j
     __shared__ double sdist[kComboTile];
+    __shared__ double2 tab[kSinTable];
+    fill_sin_table(tab);
     const int64_t t = blockIdx.x * (int64_t)blockDim.x + threadIdx.x;
     const bool valid = t < a.n;
     double4_32a tp = make_double4_32a(0, 0, 0, 0), tn = make_double4_32a(0, 0, 0, 0);
@@ -120,11 +130,11 @@ __global__ void __launch_bounds__(kComboThreads) combo_sweep_kernel(ComboArgs a)
             const double4_32a o = sp[q], on = sn[q];
             double kr, ki;
             if (!ADJ)
-                combo_kappa(a, tp.x, tp.y, tp.z, tn.x, tn.y, tn.z, tp.w, o.x, o.y, o.z, on.x, on.y, on.z, sdist[q],
-                            kr, ki);
+                combo_kappa(a, tab, tp.x, tp.y, tp.z, tn.x, tn.y, tn.z, tp.w, o.x, o.y, o.z, on.x, on.y, on.z,
+                            sdist[q], kr, ki);
             else
-                combo_kappa(a, o.x, o.y, o.z, on.x, on.y, on.z, o.w, tp.x, tp.y, tp.z, tn.x, tn.y, tn.z, td, kr,
-                            ki);
+                combo_kappa(a, tab, o.x, o.y, o.z, on.x, on.y, on.z, o.w, tp.x, tp.y, tp.z, tn.x, tn.y, tn.z, td,
+                            kr, ki);
             const double2 d = sd[q];
             if (!ADJ) {
                 ar += kr * d.x - ki * d.y;
@@ -254,6 +264,7 @@ int sweep_combo64(int64_t n, double wave, double wavenum, double eta, double tau
     a.wavenum = wavenum;
     a.eta = eta;
     a.tau = tau;
+    a.tau2 = tau * tau;
     a.pos = pos;
     a.nrm = nrm;
     a.adist = adist;

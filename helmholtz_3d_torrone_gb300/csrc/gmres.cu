@@ -239,7 +239,7 @@ int gmres_solve(LinOp &A, int64_t n, int m, const double *b_re, const double *b_
                 best = resid;
                 best_it = iters;
             }
-            if (resid < tol || hn == 0.0 || (stall > 0 && iters - best_it >= stall)) {
+            if (resid < tol || hn == 0.0 || (stall > 0 && iters - best_it >= (stall > best_it ? stall : best_it))) {
                 done = true;
                 k++;
                 break;

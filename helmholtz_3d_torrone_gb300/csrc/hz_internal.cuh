@@ -233,6 +233,16 @@ int sweep_f32_batch(int cfg, const void *desc_dev, int nops, int ncols, int64_t 
                     cudaEvent_t ev1);
 // bytes of stream-K scratch that every FP32 sweep variant fits in
 size_t sweep32_partial_bytes();
+// wave / (2 pi) split into an FP32 head (12 significant bits) and tail
+void split_wave(double wave, float &kh, float &kl);
+// FP32 products of the Combo formulation (sweep_combo32.cu) on the blocked
+// records of the annulus points; combo32_set_distances stores |d| of every
+// slot in r.nrm[].w once per build.
+int combo32_set_distances(const Rec32 &r, const double *adist, cudaStream_t s);
+int sweep_combo32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, double wavenum, double eta, int mode,
+                  const double *p_re, const double *p_im, const double *pt_re, const double *pt_im, double *q_re,
+                  double *q_im, double *qt_re, double *qt_im, float4 *dens, cudaStream_t s,
+                  cudaEvent_t ev0 = nullptr, cudaEvent_t ev1 = nullptr);
 
 }  // namespace hz
 

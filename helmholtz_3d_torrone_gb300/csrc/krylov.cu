@@ -378,6 +378,14 @@ int Krylov::reserve(int64_t n_)
     return HZ_OK;
 }
 
+int Krylov::keep_best(cudaStream_t s)
+{
+    const size_t bytes = (size_t)n * sizeof(double);
+    HZ_CHECK_CUDA(cudaMemcpyAsync(re(XB), re(X), bytes, cudaMemcpyDeviceToDevice, s));
+    HZ_CHECK_CUDA(cudaMemcpyAsync(im(XB), im(X), bytes, cudaMemcpyDeviceToDevice, s));
+    return HZ_OK;
+}
+
 double *Krylov::re(int v) { return vecs.as<double>() + (size_t)(2 * v) * n; }
 double *Krylov::im(int v) { return vecs.as<double>() + (size_t)(2 * v + 1) * n; }
 
@@ -532,11 +540,20 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
         if (err < best) {
             best = err;
             best_it = it;
-        } else if (stall > 0 && it - best_it >= stall) {
-            break;
+            if (stall > 0) HZ_TRY(keep_best(s));
+        } else if (stall > 0 && it - best_it >= (stall > best_it ? stall : best_it)) {
+            break;  // no new minimum for max(stall, best_it) iterations
         }
     }
     resid = err;
+    if (stall > 0 && best < 1e300 && !(err <= best)) {
+        // the last iterate is worse than the best one seen: return that
+        const size_t bytes = (size_t)n * sizeof(double);
+        HZ_CHECK_CUDA(cudaMemcpyAsync(re(X), re(XB), bytes, cudaMemcpyDeviceToDevice, s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(im(X), im(XB), bytes, cudaMemcpyDeviceToDevice, s));
+        resid = best;
+        if (status == HZ_ERR_NONFINITE) status = HZ_OK;
+    }
     return HZ_OK;
 }
 

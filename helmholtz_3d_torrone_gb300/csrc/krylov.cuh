@@ -48,15 +48,19 @@ struct KrylovScalars {
 
 class Krylov {
   public:
-    enum { X = 0, R, RT, P, PT, Q, QT, kVecs };
+    enum { X = 0, R, RT, P, PT, Q, QT, XB, kVecs };  // XB: best iterate of a solve with a stall limit
     // BiCGSTAB reuses slots: RH = RT (shadow), V = PT, Q = t
     enum { RH = RT, V = PT };
     ~Krylov();
     int reserve(int64_t n);
     // Solve A x = b with x0 = 0; b on the device.  Solution in re(X)/im(X).
     // stall > 0: also stop once the residual has not reached a new minimum for
-    // `stall` iterations (used by inner solves of the FP32 operator, whose
-    // rounding of the densities bounds the attainable residual near 1e-7).
+    // max(stall, iterations to the last minimum) iterations (used by inner
+    // solves of the FP32 operator, whose rounding of the densities bounds
+    // the attainable residual near 1e-7; a plateau may last as long as the
+    // progress before it),
+    // and return the iterate with the smallest residual seen (BiCG's
+    // residual can swing by orders of magnitude between iterations).
     int solve(LinOp &A, int method, const double *b_re, const double *b_im, double tol, int maxit,
               bool stagnation, bool use_graph, cudaStream_t s, int &iters, double &resid, int &status,
               int stall = 0);
@@ -67,6 +71,7 @@ class Krylov {
   private:
     int bicg_iteration(LinOp &A, cudaStream_t s);
     int stab_iteration(LinOp &A, cudaStream_t s);
+    int keep_best(cudaStream_t s);
     int64_t n = 0;
     DevBuf vecs, partial, scal;
     double *host_err = nullptr;

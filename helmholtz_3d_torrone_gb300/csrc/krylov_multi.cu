@@ -18,7 +18,7 @@ constexpr int kMT = 256;
 struct MScal {
     double rho_re, rho_im, alpha_re, alpha_im, omega_re, omega_im, beta_re, beta_im;
     double normb, err, best;
-    int active, status, it, best_it;
+    int active, status, it, best_it, improved;
 };
 
 // per-RHS partial sums of (sum a conj(b)) and ||a||^2; grid (kMB, R)
@@ -101,6 +101,7 @@ __global__ void mstart_kernel(int R, const double *partial, MScal *sc, double *h
     c.best = 1e300;
     c.it = 0;
     c.best_it = 0;
+    c.improved = 0;
     host[2 * r] = c.err;
     host[2 * r + 1] = c.active ? 1.0 : 0.0;
 }
@@ -195,6 +196,7 @@ __global__ void merr_kernel(int R, const double *partial, MScal *sc, double tol,
     const int r = threadIdx.x + blockIdx.x * blockDim.x;
     if (r >= R) return;
     MScal &c = sc[r];
+    c.improved = 0;
     if (c.active) {
         double s[3];
         msum(partial, r, s);
@@ -204,13 +206,47 @@ __global__ void merr_kernel(int R, const double *partial, MScal *sc, double tol,
         if (c.err < c.best) {
             c.best = c.err;
             c.best_it = c.it;
+            c.improved = 1;
         }
         if (c.err < tol || c.err != c.err || c.status != 0 || (stagnation && fabs(pre - c.err) < 1e-3 * tol) ||
-            (stall > 0 && c.it - c.best_it >= stall))
+            (stall > 0 && c.it - c.best_it >= max(stall, c.best_it)))
             c.active = 0;
     }
     host[2 * r] = c.err;
     host[2 * r + 1] = c.active ? 1.0 : (c.status ? -1.0 : 0.0);
+}
+
+// XB = X for the columns whose residual reached a new minimum
+__global__ void mkeep_kernel(int64_t n, const MScal *sc, const double *x_re, const double *x_im, double *b_re,
+                             double *b_im)
+{
+    if (!sc[blockIdx.y].improved) return;
+    const int64_t off = (int64_t)blockIdx.y * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        b_re[off + i] = x_re[off + i];
+        b_im[off + i] = x_im[off + i];
+    }
+}
+
+// X = XB for the columns that ended above their best residual
+__global__ void mrestore_kernel(int64_t n, const MScal *sc, double *x_re, double *x_im, const double *b_re,
+                                const double *b_im)
+{
+    const MScal c = sc[blockIdx.y];
+    if (!(c.best < 1e300) || c.err <= c.best) return;
+    const int64_t off = (int64_t)blockIdx.y * n;
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        x_re[off + i] = b_re[off + i];
+        x_im[off + i] = b_im[off + i];
+    }
+}
+
+__global__ void mresid_kernel(int R, const MScal *sc, double *host)
+{
+    const int r = threadIdx.x + blockIdx.x * blockDim.x;
+    if (r >= R) return;
+    const MScal c = sc[r];
+    host[2 * r] = (c.best < 1e300 && !(c.err <= c.best)) ? c.best : c.err;
 }
 
 int grid_x(int64_t n)
@@ -281,6 +317,10 @@ int KrylovMulti::iteration(MultiOp &A, double tol, bool stagnation, int stall, c
     HZ_CHECK_LAUNCH();
     merr_kernel<<<sb, 128, 0, s>>>(R, pp, sc, tol, stagnation ? 1 : 0, stall, host);
     HZ_CHECK_LAUNCH();
+    if (stall > 0) {
+        mkeep_kernel<<<g, kMT, 0, s>>>(n, sc, re(X), im(X), re(XB), im(XB));
+        HZ_CHECK_LAUNCH();
+    }
     return HZ_OK;
 }
 
@@ -362,6 +402,14 @@ int KrylovMulti::solve(MultiOp &A, const double *b_re, const double *b_im, doubl
             cols.swap(now);
             HZ_TRY(A.restrict_to(cols, s));
         }
+    }
+    if (stall > 0) {
+        mrestore_kernel<<<g, kMT, 0, s>>>(n, sc, re(X), im(X), re(XB), im(XB));
+        HZ_CHECK_LAUNCH();
+        mresid_kernel<<<sb, 128, 0, s>>>(R, sc, host);
+        HZ_CHECK_LAUNCH();
+        HZ_CHECK_CUDA(cudaStreamSynchronize(s));
+        for (int r = 0; r < R; r++) resid[r] = host[2 * r];
     }
     return HZ_OK;
 }

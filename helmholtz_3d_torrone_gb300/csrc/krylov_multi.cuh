@@ -30,11 +30,13 @@ struct MultiOp {
 
 class KrylovMulti {
   public:
-    enum { X = 0, RV, RH, P, V, T, kVecs };
+    enum { X = 0, RV, RH, P, V, T, XB, kVecs };  // XB: best iterates (stall > 0)
     ~KrylovMulti();
     int reserve(int64_t n, int R);
     // Solve A X = B column by column (x0 = 0); B on the device, [R][n].
     // col_iters (optional): the iterations each column took part in.
+    // stall > 0: a column also stops once its residual has not reached a new
+    // minimum for `stall` iterations, and ends on its best iterate.
     int solve(MultiOp &A, const double *b_re, const double *b_im, double tol, int maxit, bool stagnation,
               cudaStream_t s, int &iters, std::vector<double> &resid, int stall = 0,
               std::vector<int> *col_iters = nullptr);

@@ -17,16 +17,13 @@
 //
 // GB300 runs FP64 at about 1/60 of its FP32 rate, so the FP64 arithmetic is
 // kept short: 1/rho comes from rsqrt(rho^2) and rho = rho^2 / rho, and
-// sin/cos use a table-driven method (P. T. P. Tang, "Table-lookup
-// algorithms for elementary functions and their error analysis", 1991):
-// k*rho = m*(2 pi/128) + r with |r| <= pi/128, sin/cos(m 2 pi/128) from a
-// 128-entry shared table, sin/cos(r) from their Taylor series (terms to
-// r^7 and r^6; the first dropped terms are below 1e-20), recombined by the
-// angle-addition formulas.  The near-field decision keeps the reference's
-// test sqrt(rho^2) > tau exactly: it is evaluated whenever rho^2 lies
-// within a relative 1e-12 of tau^2, where rho^2 > tau^2 could disagree.
+// sin/cos use the table-driven method of sincos64.cuh.  The near-field
+// decision keeps the reference's test sqrt(rho^2) > tau exactly: it is
+// evaluated whenever rho^2 lies within a relative 1e-12 of tau^2, where
+// rho^2 > tau^2 could disagree.
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
+#include "sincos64.cuh"
 
 namespace hz {
 namespace {
@@ -62,31 +59,7 @@ __global__ void prep64_kernel(int64_t n, const double4_32a *__restrict__ nrm, co
     }
 }
 
-constexpr int kSinTable = 128;
 constexpr double kPi64 = 3.14159265358979323846264338328;
-
-// sin and cos of x >= 0 by table lookup + short series (see the header).
-__device__ __forceinline__ void table_sincos(double x, const double2 *tab, double &s, double &c)
-{
-    // 2 pi / 128 split so that m * kStepHi is exact for m < 2^22
-    const double kInvStep = 20.371832715762604;      // 128 / (2 pi)
-    const double kStepHi = 0.049087385210441425;     // 2 pi / 128 rounded to 31 significant bits
-    const double kStepLo = 1.899093908283185e-12;    // 2 pi / 128 - kStepHi
-    // nearest integer m to x * 128/(2 pi) (below 2^51): add and remove 1.5 2^52;
-    // the table index is the low word of the sum
-    const double xm = fma(x, kInvStep, 6755399441055744.0);
-    const double m = xm - 6755399441055744.0;
-    double r = fma(-m, kStepHi, x);
-    r = fma(-m, kStepLo, r);
-    const double2 t = tab[__double2loint(xm) & (kSinTable - 1)];
-    const double z = r * r;
-    // sin r = r - r^3/3! + r^5/5! - r^7/7!,  cos r = 1 - r^2/2! + r^4/4! - r^6/6!
-    const double ps = fma(fma(z, -1.0 / 5040.0, 1.0 / 120.0), z, -1.0 / 6.0);
-    const double sr = fma(r * z, ps, r);
-    const double cr = fma(fma(fma(z, -1.0 / 720.0, 1.0 / 24.0), z, -0.5), z, 1.0);
-    s = fma(t.x, cr, t.y * sr);
-    c = fma(t.y, cr, -(t.x * sr));
-}
 
 template <int MODE, bool DIR>
 __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
@@ -97,11 +70,7 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
     __shared__ alignas(128) double4_32a sd[2][T];
     __shared__ alignas(8) uint64_t bar[2];
     __shared__ double2 tab[kSinTable];
-    for (int i = threadIdx.x; i < kSinTable; i += blockDim.x) {
-        double si, co;
-        sincospi((double)i / (kSinTable / 2), &si, &co);
-        tab[i] = make_double2(si, co);
-    }
+    fill_sin_table(tab);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < a.n;
     double4_32a tp = make_double4_32a(0, 0, 0, 0), tn = make_double4_32a(0, 0, 0, 0);

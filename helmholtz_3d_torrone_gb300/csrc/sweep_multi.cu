@@ -10,6 +10,7 @@
 // cross-tile sums, with no FP64 instruction in its tile loop); the
 // densities of a tile are staged as RB/2 rows of two complex values each.
 #include "hz_internal.cuh"
+#include "sincos64.cuh"
 #include "bulk_copy.cuh"
 #include "krylov_multi.cuh"
 
@@ -200,26 +201,7 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
 }
 
 // ------------------------------------------------------------------ FP64
-constexpr int kSinTable = 128;
 constexpr int kT64m = 128;  // sources per tile = threads per block
-
-__device__ __forceinline__ void table_sincos_m(double x, const double2 *tab, double &s, double &c)
-{
-    // the same table-driven method as sweep_f64.cu
-    const double kInvStep = 20.371832715762604;
-    const double kStepHi = 0.049087385210441425;
-    const double kStepLo = 1.899093908283185e-12;
-    const double m = rint(x * kInvStep);
-    double r = fma(-m, kStepHi, x);
-    r = fma(-m, kStepLo, r);
-    const double2 t = tab[((int)m) & (kSinTable - 1)];
-    const double z = r * r;
-    const double ps = fma(fma(z, -1.0 / 5040.0, 1.0 / 120.0), z, -1.0 / 6.0);
-    const double sr = fma(r * z, ps, r);
-    const double cr = fma(fma(fma(z, -1.0 / 720.0, 1.0 / 24.0), z, -0.5), z, 1.0);
-    s = fma(t.x, cr, t.y * sr);
-    c = fma(t.y, cr, -(t.x * sr));
-}
 
 struct ArgsM64 {
     int64_t n;
@@ -263,11 +245,7 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
     extern __shared__ __align__(128) double4_32a smem64[];
     __shared__ alignas(8) uint64_t bar[2];
     __shared__ double2 tab[kSinTable];
-    for (int i = threadIdx.x; i < kSinTable; i += blockDim.x) {
-        double si, co;
-        sincospi((double)i / (kSinTable / 2), &si, &co);
-        tab[i] = make_double2(si, co);
-    }
+    fill_sin_table(tab);
     double4_32a *sp[2] = {smem64, smem64 + (2 + kRB / 2) * T};
     const double c4 = 1. / (4. * kPi);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -324,7 +302,7 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
                     const double rec = rsqrt(r2);
                     const double rho = r2 * rec;
                     double S, C;
-                    table_sincos_m(a.wave * rho, tab, S, C);
+                    table_sincos(a.wave * rho, tab, S, C);
                     const double denom = c4 * rec * rec;
                     const double ct1 = -1. * (a.wave * S + C * rec) * denom;
                     const double ct2 = (a.wave * C - S * rec) * denom;

@@ -358,9 +358,11 @@ HZ_API int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts, const double *
  * o->delta0 <= |d| <= o->epsilon (hz_dense_opts_default(HZ_DENSE_COMBO) gives
  * the driver's [0.1 H, sqrt(H)]), weights SineWeight (o->sine) or PolyWeight,
  * operator A = -i eta (dG/dn_x - 1/2) + d^2G/dn_x dn_y at offset points,
- * applied matrix free in FP64 (hz_matvec, hz_solve with HZ_PREC_F64; the FP32
- * sweeps, multi right-hand-side and gradient entries are not available for it).
- * hz_eval with HZ_COMBO_LAYER evaluates the field.  o = NULL switches back. */
+ * applied matrix free in FP64 or FP32 (hz_matvec, hz_matvec_pair, hz_solve
+ * with any precision: HZ_PREC_F32_REFINED runs FP32 products inside FP64
+ * iterative refinement; hz_autotune, the multi right-hand-side, batch and
+ * gradient entries are not available for it).  hz_eval with HZ_COMBO_LAYER
+ * evaluates the field.  o = NULL switches back. */
 HZ_API int hz_set_combo(hz_operator *op, const hz_dense_opts *o);
 
 /* Number of kernel launches made by this library in this process (graph

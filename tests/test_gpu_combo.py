@@ -135,8 +135,38 @@ def test_combo_guards(hz, combo):
     op, g, m, p, o = combo
     v = g["combo_v"]
     with pytest.raises(hz.HzError):
-        op.matvec(v, precision=hz.PREC_F32)
-    with pytest.raises(hz.HzError):
-        op.solve(v, precision=hz.PREC_F32_REFINED)
-    with pytest.raises(hz.HzError):
         op.evaluate(np.array([[1.5, 0.3, 0.2]]), v, hz.SINGLE_LAYER)
+    with pytest.raises(hz.HzError):
+        op.matvec_multi(np.stack([v, v]))
+
+
+@pytest.mark.parametrize("N", [24, 40])
+def test_combo_fp32_products(hz, N):
+    """FP32 Combo products (sweep_combo32.cu) against the FP64 ones, A and
+    A^H, on the solvable annulus (delta0 = 0.1 epsilon0)."""
+    op, p, o, d = solvable_combo(hz, N)
+    rng = np.random.default_rng(N)
+    v = rng.standard_normal(op.n) + 1j * rng.standard_normal(op.n)
+    for adj in (False, True):
+        q64 = op.matvec(v, adjoint=adj)
+        q32 = op.matvec(v, adjoint=adj, precision=hz.PREC_F32)
+        assert rel_err(q32, q64) <= 2e-5, (adj, rel_err(q32, q64))
+    q, qt = op.matvec_pair(v, v, precision=hz.PREC_F32)
+    assert rel_err(q, op.matvec(v)) <= 2e-5 and rel_err(qt, op.matvec(v, adjoint=True)) <= 2e-5
+    op.close()
+
+
+@pytest.mark.parametrize("method", ["bicgstab", "bicg", "gmres"])
+def test_combo_refined_solve(hz, method):
+    """FP32 Combo sweeps inside FP64 iterative refinement reach the dense
+    solution as the FP64 solve does (both to 1e-11)."""
+    k = 2.0
+    op, p, o, d = solvable_combo(hz, 24, k)
+    b = op.rhs_point_source(np.zeros(3), hz.RHS_MONOPOLE_NEUMANN)
+    meth = {"bicgstab": hz.BICGSTAB, "bicg": hz.BICG, "gmres": hz.GMRES}[method]
+    x, info = op.solve(b, method=meth, precision=hz.PREC_F32_REFINED, tol=1e-11, inner_tol=1e-5, maxit=2000,
+                       restart=60)
+    assert info["resid_f64"] < 1e-11 and info["outer"] >= 1
+    pts, K1, K2, rc = hz.dense_assemble(hz.DENSE_COMBO, p, o, d)
+    assert rel_err(x, np.linalg.solve(K2, b)) < 1e-8
+    op.close()
