@@ -616,11 +616,15 @@ def run_gradient(a):
             checks.append({"wrt": "%s g[%d]" % (part, i), "adjoint": float(adj), "fd": fd})
     for c in checks:
         c["rel_diff"] = abs(c["adjoint"] - c["fd"]) / max(abs(c["fd"]), 1e-300)
+        if "fd_step_1e-7" in c:
+            c["rel_diff_step_1e-7"] = abs(c["adjoint"] - c["fd_step_1e-7"]) / max(abs(c["fd_step_1e-7"]), 1e-300)
     out["fd_checks"] = checks
-    sm = [c for c in checks if c.get("smooth")]
-    out["phi_nodes_smooth"] = "%d of %d" % (len(sm), sum(1 for c in checks if "smooth" in c))
+    phi = [c for c in checks if "smooth" in c]
+    sm = [c for c in phi if c["smooth"]]
+    out["phi_nodes_smooth"] = "%d of %d" % (len(sm), len(phi))
     if sm:
         out["phi_max_rel_diff_smooth"] = max(c["rel_diff"] for c in sm)
+    out["phi_max_rel_diff_step_1e-7"] = max(c["rel_diff_step_1e-7"] for c in phi)
     out["fd_seconds"] = time.perf_counter() - t0
     out["note"] = ("J is piecewise smooth in phi: a node whose step moves a pair across the near-field radius or "
                    "flips an upwind branch of the stencils shows the jump in its difference quotient")
