@@ -39,11 +39,11 @@ if ROOT not in sys.path:
 METRIC = "256³ solve time & Gpair/s: FP32+FP64-refine vs plain FP64 GPU at 1e-6 rel err"
 FLOPS_PER_PAIR = 40  # reference pair formula, large3Dexample2.c:4471-4550
 # DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
-# 21.88 MB measured by ncu on the 128^3 torus (n = 145,272; see
+# 22.36 MB measured by ncu on the 128^3 torus (n = 145,272; see
 # profiles/sweep32_pair_torus_n128_full.md), scaled by n to n = 581,420.
 # The sweep reads every record once from DRAM and the tiles from L2, so
 # traffic grows in proportion to n.
-SWEEP32_TRAFFIC = 21.88e6 * 581420 / 145272
+SWEEP32_TRAFFIC = 22.36e6 * 581420 / 145272
 
 
 def parse():

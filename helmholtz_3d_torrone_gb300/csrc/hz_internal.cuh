@@ -233,8 +233,6 @@ int sweep_f32_batch(int cfg, const void *desc_dev, int nops, int ncols, int64_t 
                     cudaEvent_t ev1);
 // bytes of stream-K scratch that every FP32 sweep variant fits in
 size_t sweep32_partial_bytes();
-// wave / (2 pi) split into an FP32 head (12 significant bits) and tail
-void split_wave(double wave, float &kh, float &kl);
 // FP32 products of the Combo formulation (sweep_combo32.cu) on the blocked
 // records of the annulus points; combo32_set_distances stores |d| of every
 // slot in r.nrm[].w once per build.

