@@ -441,7 +441,9 @@ def run_plane_waves(a):
         out["config"] = {"workload": "torus R=0.6 r=0.25 on %d^3 over [-1,1]^3, tube |phi|<=3h, k=%g, %d incident "
                                      "plane waves e^{ik d.x} (Dirichlet data), directions on a Fibonacci sphere"
                                      % (N, wave, R), "N": N, "n_tube": n, "wave": wave, "nrhs": R,
-                         "sweep_variant": cfg, "rhs_per_kernel_pass": 8}
+                         "sweep_variant": cfg,
+                         "rhs_per_kernel_pass": "blocks of 32 (FP32) and 16 (FP64), the last block the smallest of "
+                                                "8/16/32 that holds the remaining columns"}
         # products: R right-hand sides through the multi-RHS sweep vs R single FP32 products
         op.matvec_multi(B[:8])
         t0 = time.perf_counter()

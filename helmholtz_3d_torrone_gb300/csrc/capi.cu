@@ -201,8 +201,7 @@ struct DenseOp final : LinOp {
 // Columns that stopped iterating are left out of the sweep: the others are
 // packed into consecutive columns of `pack`, swept, and their products copied
 // back (the stopped columns' products are not read).  `pairs` counts the
-// kernel evaluations (one per pair for each group of multi_rhs_block()
-// columns).
+// kernel evaluations (one per pair and kernel pass, multi_rhs_passes).
 struct MultiMatrixFreeOp final : MultiOp {
     hz_operator *op;
     int precision;
@@ -216,7 +215,7 @@ struct MultiMatrixFreeOp final : MultiOp {
         HZ_TRY(scratch->ensure(multi_rhs_scratch_bytes(op->n, op->r32.npad)));
         const int64_t n = op->n;
         const int m = cols.empty() ? R : (int)cols.size();
-        pairs += (long long)n * n * ((m + multi_rhs_block() - 1) / multi_rhs_block());
+        pairs += (long long)n * n * multi_rhs_passes(precision, m);
         if (m == R)
             return sweep_multi(sweep_const(op), op->r32, rec64(op), precision, R, p_re, p_im, q_re, q_im,
                                scratch->ptr, s);

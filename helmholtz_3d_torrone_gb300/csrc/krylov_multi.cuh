@@ -57,7 +57,8 @@ class KrylovMulti {
 };
 
 // sweep_multi.cu
-int multi_rhs_block();
+// kernel passes (one evaluation of every pair each) for nrhs columns
+long long multi_rhs_passes(int precision, int nrhs);
 size_t multi_rhs_scratch_bytes(int64_t n, int64_t npad);
 int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int precision, int nrhs,
                 const double *p_re, const double *p_im, double *q_re, double *q_im, void *scratch,

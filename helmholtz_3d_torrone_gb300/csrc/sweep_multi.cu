@@ -18,16 +18,19 @@ namespace hz {
 namespace {
 
 constexpr double kPi = 3.14159265358979323846264338328;
-constexpr int kRB = 8;  // right-hand sides per kernel pass
+// right-hand sides per kernel pass: a pass over RB columns evaluates each
+// pair once and spends 4 FMAs per column on it
+constexpr int kRBMax32 = 32;
+constexpr int kRBMax64 = 16;
 
 // ------------------------------------------------------------------ FP32
 struct ArgsM32 {
     int64_t n, npad, mwords;
-    int nr;  // right-hand sides in this pass (<= kRB)
+    int nr;  // right-hand sides in this pass (<= RB)
     float wave, tau2, guard_lo, guard_hi;
     double tau;
     const float4 *pos, *nrm;
-    const float4 *dens;  // [kRB/2][npad]: (p'_{2q} re, im, p'_{2q+1} re, im)
+    const float4 *dens;  // [RB/2][npad]: (p'_{2q} re, im, p'_{2q+1} re, im)
     const float4 *thi, *tlo, *ohi, *olo;
     const uint32_t *nearmask;
     const double4_32a *tpos, *pos64;
@@ -47,6 +50,7 @@ __device__ __forceinline__ void two_sum_m(float &hi, float &lo, float f)
     lo += e;
 }
 
+template <int RB>
 __global__ void prepm32_kernel(int64_t n, int64_t npad, int nr, const int *__restrict__ perm,
                                const double4_32a *__restrict__ tpos, const double *__restrict__ p_re,
                                const double *__restrict__ p_im, double scale, float4 *__restrict__ dens)
@@ -55,7 +59,7 @@ __global__ void prepm32_kernel(int64_t n, int64_t npad, int nr, const int *__res
         const int c = perm[s];
         const double ws = (c >= 0) ? tpos[s].w * scale : 0.0;
 #pragma unroll
-        for (int q = 0; q < kRB / 2; q++) {
+        for (int q = 0; q < RB / 2; q++) {
             float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
             if (c >= 0) {
                 const int r0 = 2 * q, r1 = 2 * q + 1;
@@ -73,10 +77,10 @@ __global__ void prepm32_kernel(int64_t n, int64_t npad, int nr, const int *__res
     }
 }
 
-template <bool DIR, bool NEAR>
+template <int RB, bool DIR, bool NEAR>
 __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, const float4 s_n, const float3 rel,
                                         const float3 tn, float treg, int64_t tslot, int64_t src_slot,
-                                        const float4 *sd, int j, float (&acc)[2 * kRB])
+                                        const float4 *sd, int j, float (&acc)[2 * RB])
 {
     const float dx = rel.x - s_p.x, dy = rel.y - s_p.y, dz = rel.z - s_p.z;
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
@@ -108,7 +112,7 @@ __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, cons
         vi = 0.f;
     }
 #pragma unroll
-    for (int q = 0; q < kRB / 2; q++) {
+    for (int q = 0; q < RB / 2; q++) {
         const float4 d = sd[q * kTile32 + j];
         acc[4 * q + 0] = fmaf(vr, d.x, fmaf(-vi, d.y, acc[4 * q + 0]));
         acc[4 * q + 1] = fmaf(vr, d.y, fmaf(vi, d.x, acc[4 * q + 1]));
@@ -118,15 +122,16 @@ __device__ __forceinline__ void pairm32(const ArgsM32 &a, const float4 s_p, cons
 }
 
 constexpr int kNT32m = 256;
-constexpr size_t kSmemM32 = 2 * (2 + kRB / 2) * kTile32 * sizeof(float4);
+template <int RB>
+constexpr size_t smem_m32() { return 2 * (2 + RB / 2) * kTile32 * sizeof(float4); }
 
-template <bool DIR>
-__global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
+template <int RB, bool DIR>
+__global__ void __launch_bounds__(kNT32m, RB <= 8 ? 2 : 1) sweepm32_kernel(ArgsM32 a)
 {
     constexpr int TS = kTile32;
     extern __shared__ __align__(128) float4 smem32[];
     __shared__ alignas(8) uint64_t bar[2];
-    float4 *sp[2] = {smem32, smem32 + (2 + kRB / 2) * TS};
+    float4 *sp[2] = {smem32, smem32 + (2 + RB / 2) * TS};
     const int64_t slot = (int64_t)blockIdx.x * kNT32m + threadIdx.x;
     const float4 th = a.thi[slot], tl = a.tlo[slot];
     const float4 nn4 = a.nrm[slot];
@@ -135,9 +140,9 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
     // near-tile mask row of this block's target tile (kNT32m == kTile32)
     const uint32_t *mrow = a.nearmask + (slot / TS) * a.mwords;
     // cross-tile sums: FP32 head + tail (TwoSum)
-    float acch[2 * kRB], accl[2 * kRB];
+    float acch[2 * RB], accl[2 * RB];
 #pragma unroll
-    for (int i = 0; i < 2 * kRB; i++) acch[i] = accl[i] = 0.f;
+    for (int i = 0; i < 2 * RB; i++) acch[i] = accl[i] = 0.f;
     const int64_t ntiles = a.npad / TS;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -148,11 +153,11 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
     auto issue = [&](int64_t tile, int buf) {
         const int64_t base = tile * TS;
         const uint32_t bytes = TS * sizeof(float4);
-        mbar_arrive_expect_tx(&bar[buf], (2 + kRB / 2) * bytes);
+        mbar_arrive_expect_tx(&bar[buf], (2 + RB / 2) * bytes);
         bulk_g2s(sp[buf], a.pos + base, bytes, &bar[buf]);
         bulk_g2s(sp[buf] + TS, a.nrm + base, bytes, &bar[buf]);
 #pragma unroll
-        for (int q = 0; q < kRB / 2; q++) bulk_g2s(sp[buf] + (2 + q) * TS, a.dens + q * a.npad + base, bytes, &bar[buf]);
+        for (int q = 0; q < RB / 2; q++) bulk_g2s(sp[buf] + (2 + q) * TS, a.dens + q * a.npad + base, bytes, &bar[buf]);
     };
     if (threadIdx.x == 0) issue(0, 0);
     for (int64_t tile = 0; tile < ntiles; tile++) {
@@ -171,23 +176,25 @@ __global__ void __launch_bounds__(kNT32m, 2) sweepm32_kernel(ArgsM32 a)
             return;
         }
         const float4 *P = sp[buf], *Nn = sp[buf] + TS, *D = sp[buf] + 2 * TS;
-        float acc[2 * kRB];
+        float acc[2 * RB];
 #pragma unroll
-        for (int i = 0; i < 2 * kRB; i++) acc[i] = 0.f;
+        for (int i = 0; i < 2 * RB; i++) acc[i] = 0.f;
         const int64_t base = tile * TS;
         if (far) {
-            for (int j = 0; j < TS; j++) pairm32<DIR, false>(a, P[j], Nn[j], rel, tn, treg, slot, base + j, D, j, acc);
+            for (int j = 0; j < TS; j++)
+                pairm32<RB, DIR, false>(a, P[j], Nn[j], rel, tn, treg, slot, base + j, D, j, acc);
         } else {
-            for (int j = 0; j < TS; j++) pairm32<DIR, true>(a, P[j], Nn[j], rel, tn, treg, slot, base + j, D, j, acc);
+            for (int j = 0; j < TS; j++)
+                pairm32<RB, DIR, true>(a, P[j], Nn[j], rel, tn, treg, slot, base + j, D, j, acc);
         }
 #pragma unroll
-        for (int i = 0; i < 2 * kRB; i++) two_sum_m(acch[i], accl[i], acc[i]);
+        for (int i = 0; i < 2 * RB; i++) two_sum_m(acch[i], accl[i], acc[i]);
         __syncthreads();
     }
     const int c = a.perm[slot];
     if (c < 0) return;
 #pragma unroll
-    for (int r = 0; r < kRB; r++) {
+    for (int r = 0; r < RB; r++) {
         if (r >= a.nr) break;
         const double vr = (double)acch[2 * r] + (double)accl[2 * r];
         const double vi = (double)acch[2 * r + 1] + (double)accl[2 * r + 1];
@@ -205,19 +212,20 @@ struct ArgsM64 {
     int nr;
     double wave, tau, tau2, sg;
     const double4_32a *pos, *nrm;
-    const double4_32a *dens;  // [kRB/2][n]: (w p_{2q}, w p_{2q+1})
+    const double4_32a *dens;  // [RB/2][n]: (w p_{2q}, w p_{2q+1})
     const double *p_re, *p_im;
     double *q_re, *q_im;
     unsigned *err;
 };
 
+template <int RB>
 __global__ void prepm64_kernel(int64_t n, int nr, const double4_32a *__restrict__ nrm, const double *__restrict__ p_re,
                                const double *__restrict__ p_im, double4_32a *__restrict__ dens)
 {
     for (int64_t s = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
         const double w = nrm[s].w;
 #pragma unroll
-        for (int q = 0; q < kRB / 2; q++) {
+        for (int q = 0; q < RB / 2; q++) {
             const int r0 = 2 * q, r1 = 2 * q + 1;
             double4_32a v = make_double4_32a(0, 0, 0, 0);
             if (r0 < nr) {
@@ -233,9 +241,10 @@ __global__ void prepm64_kernel(int64_t n, int nr, const double4_32a *__restrict_
     }
 }
 
-constexpr size_t kSmemM64 = 2 * (2 + kRB / 2) * kT64m * sizeof(double4_32a);
+template <int RB>
+constexpr size_t smem_m64() { return 2 * (2 + RB / 2) * kT64m * sizeof(double4_32a); }
 
-template <bool DIR>
+template <int RB, bool DIR>
 __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
 {
     constexpr int T = kT64m;
@@ -243,7 +252,7 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
     __shared__ alignas(8) uint64_t bar[2];
     __shared__ double2 tab[kSinTable];
     fill_sin_table(tab);
-    double4_32a *sp[2] = {smem64, smem64 + (2 + kRB / 2) * T};
+    double4_32a *sp[2] = {smem64, smem64 + (2 + RB / 2) * T};
     const double c4 = 1. / (4. * kPi);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool valid = t < a.n;
@@ -252,9 +261,9 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
         tp = a.pos[t];
         tn = a.nrm[t];
     }
-    double acc[2 * kRB];
+    double acc[2 * RB];
 #pragma unroll
-    for (int i = 0; i < 2 * kRB; i++) acc[i] = 0.0;
+    for (int i = 0; i < 2 * RB; i++) acc[i] = 0.0;
     const int64_t ntiles = (a.n + T - 1) / T;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -266,11 +275,11 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
         const int64_t base = tile * T;
         const int64_t cnt = (a.n - base < T) ? (a.n - base) : T;
         const uint32_t bytes = (uint32_t)(cnt * sizeof(double4_32a));
-        mbar_arrive_expect_tx(&bar[buf], (2 + kRB / 2) * bytes);
+        mbar_arrive_expect_tx(&bar[buf], (2 + RB / 2) * bytes);
         bulk_g2s(sp[buf], a.pos + base, bytes, &bar[buf]);
         bulk_g2s(sp[buf] + T, a.nrm + base, bytes, &bar[buf]);
 #pragma unroll
-        for (int q = 0; q < kRB / 2; q++) bulk_g2s(sp[buf] + (2 + q) * T, a.dens + q * a.n + base, bytes, &bar[buf]);
+        for (int q = 0; q < RB / 2; q++) bulk_g2s(sp[buf] + (2 + q) * T, a.dens + q * a.n + base, bytes, &bar[buf]);
     };
     if (threadIdx.x == 0 && ntiles > 0) issue(0, 0);
     for (int64_t tile = 0; tile < ntiles; tile++) {
@@ -312,7 +321,7 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
                     vi = 0.0;
                 }
 #pragma unroll
-                for (int q = 0; q < kRB / 2; q++) {
+                for (int q = 0; q < RB / 2; q++) {
                     const double4_32a d = D[q * T + j];
                     acc[4 * q + 0] += vr * d.x - vi * d.y;
                     acc[4 * q + 1] += vr * d.y + vi * d.x;
@@ -325,7 +334,7 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
     }
     if (!valid) return;
 #pragma unroll
-    for (int r = 0; r < kRB; r++) {
+    for (int r = 0; r < RB; r++) {
         if (r >= a.nr) break;
         const double vr = acc[2 * r], vi = acc[2 * r + 1];
         if (!isfinite(vr) || !isfinite(vi)) atomicOr(a.err, DEV_ERR_NONFINITE);
@@ -341,15 +350,107 @@ int blocks_for(int64_t work)
     return (int)(b < 1 ? 1 : b);
 }
 
+// Block of the next pass for `left` remaining columns: the smallest compiled
+// block that holds them all, else the largest (one pass over RB columns
+// costs about c0 + c1 RB, so a wider block beats two narrower passes).
+int pass_block(int precision, int left)
+{
+    const int top = (precision == HZ_PREC_F64) ? kRBMax64 : kRBMax32;
+    for (int rb = 8; rb < top; rb *= 2)
+        if (left <= rb) return rb;
+    return top;
+}
+
+template <int RB>
+int launch_m64(const SweepConst &c, const Rec64 &r64, int nr, const double *pr, const double *pi, double *qr,
+               double *qi, void *scratch, cudaStream_t s)
+{
+    constexpr int smem = (int)smem_m64<RB>();
+    HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<RB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<RB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    double4_32a *dens = static_cast<double4_32a *>(scratch);
+    prepm64_kernel<RB><<<blocks_for(c.n), 256, 0, s>>>(c.n, nr, r64.nrm, pr, pi, dens);
+    HZ_CHECK_LAUNCH();
+    ArgsM64 a;
+    a.n = c.n;
+    a.nr = nr;
+    a.wave = c.wave;
+    a.tau = c.tau;
+    a.tau2 = c.tau * c.tau;
+    a.sg = (c.interior == 1) ? -1.0 : 1.0;
+    a.pos = r64.pos;
+    a.nrm = r64.nrm;
+    a.dens = dens;
+    a.p_re = pr;
+    a.p_im = pi;
+    a.q_re = qr;
+    a.q_im = qi;
+    a.err = c.err;
+    const unsigned blocks = (unsigned)((c.n + kT64m - 1) / kT64m);
+    if (c.dirichlet) sweepm64_kernel<RB, true><<<blocks, kT64m, smem, s>>>(a);
+    else sweepm64_kernel<RB, false><<<blocks, kT64m, smem, s>>>(a);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
+template <int RB>
+int launch_m32(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int nr, const double *pr, const double *pi,
+               double *qr, double *qi, void *scratch, cudaStream_t s)
+{
+    constexpr int smem = (int)smem_m32<RB>();
+    HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm32_kernel<RB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm32_kernel<RB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
+    float4 *dens = static_cast<float4 *>(scratch);
+    const double scale = ((c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi);
+    prepm32_kernel<RB><<<blocks_for(r32.npad), 256, 0, s>>>(c.n, r32.npad, nr, r32.perm, r32.tpos, pr, pi, scale,
+                                                            dens);
+    HZ_CHECK_LAUNCH();
+    ArgsM32 a;
+    a.n = c.n;
+    a.npad = r32.npad;
+    a.nr = nr;
+    a.wave = (float)c.wave;
+    a.tau = c.tau;
+    a.mwords = r32.mwords;
+    a.tau2 = (float)(c.tau * c.tau);
+    a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
+    a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
+    a.pos = r32.pos;
+    a.nrm = r32.nrm;
+    a.dens = dens;
+    a.thi = r32.thi;
+    a.tlo = r32.tlo;
+    a.ohi = r32.ohi;
+    a.olo = r32.olo;
+    a.nearmask = r32.nearmask;
+    a.tpos = r32.tpos;
+    a.pos64 = r64.pos;
+    a.perm = r32.perm;
+    a.p_re = pr;
+    a.p_im = pi;
+    a.q_re = qr;
+    a.q_im = qi;
+    a.err = c.err;
+    const unsigned blocks = (unsigned)(r32.npad / kNT32m);
+    if (c.dirichlet) sweepm32_kernel<RB, true><<<blocks, kNT32m, smem, s>>>(a);
+    else sweepm32_kernel<RB, false><<<blocks, kNT32m, smem, s>>>(a);
+    HZ_CHECK_LAUNCH();
+    return HZ_OK;
+}
+
 }  // namespace
 
-
-int multi_rhs_block() { return kRB; }
+long long multi_rhs_passes(int precision, int nrhs)
+{
+    long long p = 0;
+    for (int r0 = 0; r0 < nrhs; r0 += pass_block(precision, nrhs - r0)) p++;
+    return p;
+}
 
 size_t multi_rhs_scratch_bytes(int64_t n, int64_t npad)
 {
-    const size_t a = (size_t)(kRB / 2) * (size_t)npad * sizeof(float4);
-    const size_t b = (size_t)(kRB / 2) * (size_t)n * sizeof(double4_32a);
+    const size_t a = (size_t)(kRBMax32 / 2) * (size_t)npad * sizeof(float4);
+    const size_t b = (size_t)(kRBMax64 / 2) * (size_t)n * sizeof(double4_32a);
     return a > b ? a : b;
 }
 
@@ -358,78 +459,20 @@ int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int pre
                 cudaStream_t s)
 {
     if (c.n <= 0 || nrhs <= 0) return HZ_OK;
-    for (int r0 = 0; r0 < nrhs; r0 += kRB) {
-        const int nr = (nrhs - r0 < kRB) ? (nrhs - r0) : kRB;
+    for (int r0 = 0; r0 < nrhs;) {
+        const int rb = pass_block(precision, nrhs - r0);
+        const int nr = (nrhs - r0 < rb) ? (nrhs - r0) : rb;
         const double *pr = p_re + (int64_t)r0 * c.n, *pi = p_im + (int64_t)r0 * c.n;
         double *qr = q_re + (int64_t)r0 * c.n, *qi = q_im + (int64_t)r0 * c.n;
         if (precision == HZ_PREC_F64) {
-            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kSmemM64));
-            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kSmemM64));
-            double4_32a *dens = static_cast<double4_32a *>(scratch);
-            prepm64_kernel<<<blocks_for(c.n), 256, 0, s>>>(c.n, nr, r64.nrm, pr, pi, dens);
-            HZ_CHECK_LAUNCH();
-            ArgsM64 a;
-            a.n = c.n;
-            a.nr = nr;
-            a.wave = c.wave;
-            a.tau = c.tau;
-            a.tau2 = c.tau * c.tau;
-            a.sg = (c.interior == 1) ? -1.0 : 1.0;
-            a.pos = r64.pos;
-            a.nrm = r64.nrm;
-            a.dens = dens;
-            a.p_re = pr;
-            a.p_im = pi;
-            a.q_re = qr;
-            a.q_im = qi;
-            a.err = c.err;
-            const unsigned blocks = (unsigned)((c.n + kT64m - 1) / kT64m);
-            if (c.dirichlet) sweepm64_kernel<true><<<blocks, kT64m, kSmemM64, s>>>(a);
-            else sweepm64_kernel<false><<<blocks, kT64m, kSmemM64, s>>>(a);
-            HZ_CHECK_LAUNCH();
+            if (rb == 8) HZ_TRY(launch_m64<8>(c, r64, nr, pr, pi, qr, qi, scratch, s));
+            else HZ_TRY(launch_m64<16>(c, r64, nr, pr, pi, qr, qi, scratch, s));
         } else {
-            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm32_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kSmemM32));
-            HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm32_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                               (int)kSmemM32));
-            float4 *dens = static_cast<float4 *>(scratch);
-            const double scale = ((c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi);
-            prepm32_kernel<<<blocks_for(r32.npad), 256, 0, s>>>(c.n, r32.npad, nr, r32.perm, r32.tpos, pr, pi, scale,
-                                                                dens);
-            HZ_CHECK_LAUNCH();
-            ArgsM32 a;
-            a.n = c.n;
-            a.npad = r32.npad;
-            a.nr = nr;
-            a.wave = (float)c.wave;
-            a.tau = c.tau;
-            a.mwords = r32.mwords;
-            a.tau2 = (float)(c.tau * c.tau);
-            a.guard_lo = (float)(c.tau * c.tau * (1.0 - 1e-4));
-            a.guard_hi = (float)(c.tau * c.tau * (1.0 + 1e-4));
-            a.pos = r32.pos;
-            a.nrm = r32.nrm;
-            a.dens = dens;
-            a.thi = r32.thi;
-            a.tlo = r32.tlo;
-            a.ohi = r32.ohi;
-            a.olo = r32.olo;
-            a.nearmask = r32.nearmask;
-            a.tpos = r32.tpos;
-            a.pos64 = r64.pos;
-            a.perm = r32.perm;
-            a.p_re = pr;
-            a.p_im = pi;
-            a.q_re = qr;
-            a.q_im = qi;
-            a.err = c.err;
-            const unsigned blocks = (unsigned)(r32.npad / kNT32m);
-            if (c.dirichlet) sweepm32_kernel<true><<<blocks, kNT32m, kSmemM32, s>>>(a);
-            else sweepm32_kernel<false><<<blocks, kNT32m, kSmemM32, s>>>(a);
-            HZ_CHECK_LAUNCH();
+            if (rb == 8) HZ_TRY(launch_m32<8>(c, r32, r64, nr, pr, pi, qr, qi, scratch, s));
+            else if (rb == 16) HZ_TRY(launch_m32<16>(c, r32, r64, nr, pr, pi, qr, qi, scratch, s));
+            else HZ_TRY(launch_m32<32>(c, r32, r64, nr, pr, pi, qr, qi, scratch, s));
         }
+        r0 += nr;
     }
     return HZ_OK;
 }

@@ -173,7 +173,8 @@ HZ_API int hz_matvec_pair(hz_operator *op, int precision, const double *p_re, co
                    double *qt_re, double *qt_im, int where);
 /* Multi right-hand side: Q = A P for nrhs column vectors stored one after
  * the other (vector r at offset r*n), one kernel evaluation per pair and
- * block of 8 right-hand sides. */
+ * kernel pass; a pass takes a block of 8, 16 or 32 right-hand sides (FP64:
+ * 8 or 16), the smallest block that holds the remaining columns. */
 HZ_API int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re,
                     const double *p_im, double *q_re, double *q_im, int where);
 
