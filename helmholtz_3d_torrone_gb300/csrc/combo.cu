@@ -29,7 +29,7 @@ constexpr int kComboTile = 128;
 
 struct ComboArgs {
     int64_t n;
-    double wave, wavenum, eta, tau, tau2;
+    double wave, wavenum, k2, eta, tau, tau2;
     const double4_32a *pos;  // (x*, reg)
     const double4_32a *nrm;  // (n, r)
     const double *adist;     // |d|
@@ -79,17 +79,16 @@ __device__ __forceinline__ void combo_kappa(const ComboArgs &a, const double2 *t
     const double cm2 = ip2 * rn * ip3 * rn;
     double s0, c0;
     table_sincos(k * yn, tab, s0, c0);
-    const double cv = c0 * rn, sv = s0 * rn;
-    const double t1r = -1. * (cv * rn + k * sv) * cm1;
-    const double t1i = (k * cv - sv * rn) * cm1;
-    const double t2r = -1. * k * k * cv * cm2;
-    const double t2i = -1. * k * k * sv * cm2;
-    const double t3r = 3. * k * sv * cm2 * rn;
-    const double t3i = -3. * k * cv * cm2 * rn;
-    const double t4r = 3. * cv * rn * cm2 * rn;
-    const double t4i = 3. * sv * rn * cm2 * rn;
-    kr = a.eta * parti + (t1r + t2r + t3r + t4r) * c4;
-    ki = -1. * a.eta * part + (t1i + t2i + t3i + t4i) * c4;
+    // the reference's four terms t1..t4 (HelmholtzKernel.c:539-571)
+    // regrouped: with e1 = k sin + cos/|y| and e2 = k cos - sin/|y|,
+    //   t1 + .. + t4 = (1/|y|) [-cm1 e1 + cm2 (3 e1/|y| - k^2 cos)]  (real)
+    //                  (1/|y|) [ cm1 e2 - cm2 (3 e2/|y| + k^2 sin)]  (imaginary)
+    const double e1 = c0 * rn + k * s0, e2 = k * c0 - s0 * rn;
+    const double g3 = 3. * rn;
+    const double tr = rn * (cm2 * (g3 * e1 - a.k2 * c0) - cm1 * e1);
+    const double ti = rn * (cm1 * e2 - cm2 * (g3 * e2 + a.k2 * s0));
+    kr = a.eta * parti + tr * c4;
+    ki = -1. * a.eta * part + ti * c4;
 }
 
 // One thread per output point; the other points come through shared
@@ -262,6 +261,7 @@ int sweep_combo64(int64_t n, double wave, double wavenum, double eta, double tau
     a.n = n;
     a.wave = wave;
     a.wavenum = wavenum;
+    a.k2 = wavenum * wavenum;
     a.eta = eta;
     a.tau = tau;
     a.tau2 = tau * tau;
