@@ -24,6 +24,7 @@ HZ_HOST, HZ_DEVICE = 0, 1
 PREC_F64, PREC_F32, PREC_F32_REFINED = 0, 1, 2
 BICG, BICGSTAB, GMRES = 0, 1, 2
 SINGLE_LAYER, DOUBLE_LAYER, COMBO_LAYER = 0, 1, 2
+PHASE_DIRECT, PHASE_SPLIT = 0, 1
 RHS_POINT_DIRICHLET, RHS_POINT_NEUMANN, RHS_MONOPOLE_NEUMANN, RHS_MONOPOLE_DIRICHLET = 0, 1, 2, 3
 NOALLOC_MAX_POINTS = 32768  # HZ_NOALLOC_MAX_POINTS
 
@@ -108,6 +109,7 @@ SIGNATURES = {
     "hz_sweep_timing": ([_vp, C.c_int, _dp, C.POINTER(C.c_int64)], C.c_int),
     "hz_autotune": ([_vp, C.POINTER(C.c_int), _dp], C.c_int),
     "hz_set_sweep_config": ([_vp, C.c_int], C.c_int),
+    "hz_set_phase_mode": ([_vp, C.c_int], C.c_int),
     "hz_get_grids": ([_vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_get_tube": ([_vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_matvec": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
@@ -282,6 +284,10 @@ class Operator:
 
     def set_sweep_config(self, cfg):
         _check(load().hz_set_sweep_config(self.h, cfg))
+
+    def set_phase_mode(self, mode):
+        """PHASE_DIRECT (default) or PHASE_SPLIT for the FP32 pair sweep."""
+        _check(load().hz_set_phase_mode(self.h, mode))
 
     def sweep_timing(self, enable=-1):
         """Enable (1) / disable (0) per-sweep CUDA-event timing, or read (-1):

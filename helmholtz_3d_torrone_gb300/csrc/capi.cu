@@ -85,6 +85,7 @@ SweepConst sweep_const(const hz_operator *op)
     c.dirichlet = op->p.dirichlet;
     c.interior = op->p.interior;
     c.err = op->err.as<unsigned>();
+    c.phase_split = op->phase_mode == HZ_PHASE_SPLIT;
     return c;
 }
 
@@ -160,7 +161,8 @@ struct MatrixFreeOp final : LinOp {
     }
     uint64_t key() const override
     {
-        return ((uint64_t)(uintptr_t)op << 8) ^ (uint64_t)(precision * 16 + op->sweep_cfg) ^ 1ull;
+        return ((uint64_t)(uintptr_t)op << 8) ^ (uint64_t)(precision * 16 + op->sweep_cfg) ^
+               ((uint64_t)op->phase_mode << 6) ^ 1ull;
     }
 };
 
@@ -431,6 +433,16 @@ static int need_classic(hz_operator *op, const char *who)
 extern "C" {
 
 const char *hz_last_error(void) { return g_err; }
+
+int hz_set_phase_mode(hz_operator *op, int mode)
+{
+    if (!op || (mode != HZ_PHASE_DIRECT && mode != HZ_PHASE_SPLIT)) {
+        set_error("hz_set_phase_mode: need an operator and HZ_PHASE_DIRECT or HZ_PHASE_SPLIT");
+        return HZ_ERR_ARG;
+    }
+    op->phase_mode = mode;
+    return HZ_OK;
+}
 
 int hz_set_combo(hz_operator *op, const hz_dense_opts *o)
 {

@@ -119,6 +119,7 @@ struct SweepConst {
     int dirichlet;
     int interior;
     unsigned *err;  // device error word
+    int phase_split = 0;  // FP32 sweep: phase reduced with a split k/(2 pi) (HZ_PHASE_SPLIT)
 };
 
 // sweep modes
@@ -270,6 +271,7 @@ struct hz_operator {
     hz_solver_state *solver = nullptr;  // Krylov workspaces (capi.cu)
     hz::SweepTimer timer;
     int sweep_cfg = 0;  // FP32 sweep variant (hz_autotune)
+    int phase_mode = 0; // HZ_PHASE_DIRECT or HZ_PHASE_SPLIT (hz_set_phase_mode)
     // Combo formulation (hz_set_combo): annulus points, FP64 products only
     int combo = 0;
     hz_dense_opts combo_opts{};

@@ -15,8 +15,9 @@
 //    rad times k rho either way.  The FP32 product then stays within
 //    1e-7 of the FP64 product (4.5e-8 on the 256^3 torus at k = 20,
 //    3.3e-7 on 128^3 at k = 40), far below the 1e-5 inner tolerance.
-//    Reducing the phase in revolutions with a split k/(2 pi) first halved
-//    that error but cost 6 % of the sweep's throughput.
+//    Reducing the phase in revolutions with a split k/(2 pi) first
+//    (hz_set_phase_mode(op, HZ_PHASE_SPLIT), the MODE bit
+//    SWEEP_PHASE_SPLIT) halves that error at 6 % of the throughput.
 //  * The near-field test rho <= tau is decided in FP64 (with the FP64
 //    sweep's own arithmetic) whenever the FP32 rho^2 lies within 1e-4 of
 //    tau^2, so FP32 and FP64 operators classify every pair alike.
@@ -45,9 +46,13 @@ namespace {
 
 constexpr double kPi = 3.14159265358979323846264338328;
 
+// Internal MODE bit: reduce the phase in revolutions with a split k/(2 pi)
+// (hz_set_phase_mode, HZ_PHASE_SPLIT) instead of passing k rho to the SFU.
+constexpr int SWEEP_PHASE_SPLIT = 4;
+
 struct Args32 {
     int64_t n, npad, mwords;
-    float wave;
+    float wave, kh, kl;  // k and k/(2 pi) = kh + kl (kh: 12 significant bits)
     float tau2, guard_lo, guard_hi;
     double tau;
     const float4 *pos, *nrm, *dens;
@@ -136,7 +141,16 @@ __device__ __forceinline__ void pair_block(const Args32 &a, const float4 s_p, co
         const float rinv = rsqrtf(r2);
         const float rho = r2 * rinv;
         float S, C;
-        __sincosf(rho * a.wave, &S, &C);
+        if (MODE & SWEEP_PHASE_SPLIT) {
+            // revolutions rho k/(2 pi) less the nearest integer (|rho kh| <
+            // 2^22: add and remove 1.5 2^23), exact to ~2^-24 before the SFU
+            const float nn = fmaf(rho, a.kh, 12582912.f) - 12582912.f;
+            float f = fmaf(rho, a.kh, -nn);
+            f = fmaf(rho, a.kl, f);
+            __sincosf(f * 6.28318530717958647692f, &S, &C);
+        } else {
+            __sincosf(rho * a.wave, &S, &C);
+        }
         const float u1 = fmaf(C, rinv, a.wave * S);   // k sin + cos/rho
         const float u2 = fmaf(a.wave, C, -S * rinv);  // k cos - sin/rho
         const float rr = rinv * rinv;
@@ -677,6 +691,16 @@ int launch32(int cfg, const Args32 &a, bool dir, size_t pb, cudaStream_t s)
 }  // namespace
 
 // Split k/(2 pi) into a head with 12 significant bits and an FP32 tail.
+void split_wave(double wave, float &kh, float &kl)
+{
+    const double kc = wave / (2.0 * kPi);
+    int e;
+    frexp(kc, &e);
+    const double q = ldexp(1.0, e - 12);
+    const double head = nearbyint(kc / q) * q;
+    kh = (float)head;
+    kl = (float)(kc - head);
+}
 
 double sweep32_reg_scale(int interior) { return ((interior == 1) ? -1.0 : 1.0) * (4.0 * kPi); }
 
@@ -701,9 +725,13 @@ size_t partial_need_all()
 
 size_t sweep32_partial_bytes()
 {
-    const size_t v[6] = {partial_need_all<SWEEP_A, false>(),    partial_need_all<SWEEP_A, true>(),
-                         partial_need_all<SWEEP_AH, false>(),   partial_need_all<SWEEP_AH, true>(),
-                         partial_need_all<SWEEP_PAIR, false>(), partial_need_all<SWEEP_PAIR, true>()};
+    constexpr int S = SWEEP_PHASE_SPLIT;
+    const size_t v[12] = {partial_need_all<SWEEP_A, false>(),        partial_need_all<SWEEP_A, true>(),
+                          partial_need_all<SWEEP_AH, false>(),       partial_need_all<SWEEP_AH, true>(),
+                          partial_need_all<SWEEP_PAIR, false>(),     partial_need_all<SWEEP_PAIR, true>(),
+                          partial_need_all<SWEEP_A | S, false>(),    partial_need_all<SWEEP_A | S, true>(),
+                          partial_need_all<SWEEP_AH | S, false>(),   partial_need_all<SWEEP_AH | S, true>(),
+                          partial_need_all<SWEEP_PAIR | S, false>(), partial_need_all<SWEEP_PAIR | S, true>()};
     size_t m = 0;
     for (size_t x : v) m = x > m ? x : m;
     return m;
@@ -848,9 +876,18 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     a.err = c.err;
     if (ev0) HZ_CHECK_CUDA(record_timing_event(ev0, s));
     a.partial = r.partial;
-    if (mode == SWEEP_PAIR) HZ_TRY(launch32<SWEEP_PAIR>(cfg, a, c.dirichlet != 0, r.partial_bytes, s));
-    else if (mode == SWEEP_A) HZ_TRY(launch32<SWEEP_A>(cfg, a, c.dirichlet != 0, r.partial_bytes, s));
-    else HZ_TRY(launch32<SWEEP_AH>(cfg, a, c.dirichlet != 0, r.partial_bytes, s));
+    split_wave(c.wave, a.kh, a.kl);
+    const bool dir = c.dirichlet != 0;
+    constexpr int S = SWEEP_PHASE_SPLIT;
+    if (c.phase_split) {
+        if (mode == SWEEP_PAIR) HZ_TRY(launch32<SWEEP_PAIR | S>(cfg, a, dir, r.partial_bytes, s));
+        else if (mode == SWEEP_A) HZ_TRY(launch32<SWEEP_A | S>(cfg, a, dir, r.partial_bytes, s));
+        else HZ_TRY(launch32<SWEEP_AH | S>(cfg, a, dir, r.partial_bytes, s));
+    } else {
+        if (mode == SWEEP_PAIR) HZ_TRY(launch32<SWEEP_PAIR>(cfg, a, dir, r.partial_bytes, s));
+        else if (mode == SWEEP_A) HZ_TRY(launch32<SWEEP_A>(cfg, a, dir, r.partial_bytes, s));
+        else HZ_TRY(launch32<SWEEP_AH>(cfg, a, dir, r.partial_bytes, s));
+    }
     if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
     return HZ_OK;
 }

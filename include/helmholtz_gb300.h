@@ -148,6 +148,17 @@ HZ_API int64_t hz_tube_size(const hz_operator *op);
 HZ_API int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep);
 HZ_API int hz_set_sweep_config(hz_operator *op, int cfg);
 
+/* Phase of the FP32 pair sweep (hz_matvec, hz_matvec_pair and the FP32
+ * products of hz_solve).  HZ_PHASE_DIRECT (default): k rho goes to the SFU's
+ * sin/cos as one FP32 product.  HZ_PHASE_SPLIT: the phase is first reduced in
+ * revolutions with k/(2 pi) split into an FP32 head and tail, which about
+ * halves the FP32-vs-FP64 product error (e.g. 4.5e-8 -> 2.9e-8 on a 256^3
+ * torus at k = 20) at about 6 % of the sweep's throughput.  The multi
+ * right-hand-side, batch and Combo FP32 sweeps use the direct phase. */
+#define HZ_PHASE_DIRECT 0
+#define HZ_PHASE_SPLIT 1
+HZ_API int hz_set_phase_mode(hz_operator *op, int mode);
+
 /* Per-kernel timing of the pair sweeps: CUDA events recorded on the launch
  * stream around every sweep kernel (also inside the solver's iteration
  * graphs).  enable = 1 / 0 switches it on / off and clears the totals,

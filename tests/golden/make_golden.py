@@ -32,7 +32,7 @@ CASES = {
                                    center=(0.013, 0.021, 0.007), rhs_kind=2),
     "ref_neumann_sphere_n24": dict(variant="neumann", N=24, wave=5.0, shape="sphere", radius=1.0,
                                    center=(0.013, 0.021, 0.007), rhs_kind=2),
-    # the BASELINE domain and formulation: [-1,1]^3, FACTOR 3, Dirichlet
+    # the benchmark domain and formulation: [-1,1]^3, FACTOR 3, Dirichlet
     "ref_dirichlet_sphere_n20": dict(variant="dirichlet", N=20, wave=5.0, shape="sphere", radius=0.5,
                                      center=(0.0, 0.0, 0.0), rhs_kind=0),
     # a torus small enough for a dense reference run (R=0.5, r=0.25 keeps

@@ -179,3 +179,35 @@ def test_dense_bicg_vs_reference(hz):
     are, aim = o.dense(p, tp)
     x, info = hz.dense_bicg(are + 1j * aim, g["b"], tol=1e-13, maxit=1000)
     assert rel_err(x, g["x"]) < 1e-10
+
+
+def test_phase_split_mode(hz):
+    """hz_set_phase_mode: the FP32 sweep with the phase reduced through a
+    split k/(2 pi) stays within the FP32 bound of the FP64 product (A, A^H
+    and the fused pair), and a refined solve in that mode equals the FP64
+    solve."""
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    N, k = 32, 20.0
+    p = hz.params(N, k, int_l=-1.0, int_u=1.0, factor=3.0, dirichlet=1)
+    with hz.Operator(p) as op:
+        # the multi right-hand-side tests' torus: on this grid every
+        # projected point and its interpolation cell lie inside [-1,1]^3
+        op.set_distance(G.torus(N, R=0.5, r=0.25))
+        op.build()
+        rng = np.random.default_rng(7)
+        v = rng.standard_normal(op.n) + 1j * rng.standard_normal(op.n)
+        q64, qt64 = op.matvec(v), op.matvec(v, adjoint=True)
+        errs = {}
+        for mode in (hz.PHASE_DIRECT, hz.PHASE_SPLIT):
+            op.set_phase_mode(mode)
+            q, qt = op.matvec_pair(v, v, precision=hz.PREC_F32)
+            assert rel_err(q, q64) <= 2e-5 and rel_err(qt, qt64) <= 2e-5
+            assert rel_err(op.matvec(v, precision=hz.PREC_F32), q64) <= 2e-5
+            errs[mode] = rel_err(q, q64)
+        op.set_phase_mode(hz.PHASE_SPLIT)
+        b = op.rhs_point_source(np.array([0.5, 0.0, 0.0]), hz.RHS_POINT_DIRICHLET)
+        x, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F32_REFINED, tol=1e-11)
+        x64, _ = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=1e-12)
+        assert rel_err(x, x64) < 1e-8
+        with pytest.raises(hz.HzError):
+            op.set_phase_mode(2)
