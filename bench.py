@@ -88,6 +88,10 @@ def parse():
     ap.add_argument("--batch", type=int, default=0,
                     help="instead of the step benchmark: solve this many seeded ellipsoids (semi-axes U[0.2,0.7], "
                          "grids 64^3-192^3) as one batch and one after another, and report both times")
+    ap.add_argument("--batch-grids", type=int, nargs="*", default=[64, 96, 128, 160, 192],
+                    help="--batch: grid sizes drawn per surface")
+    ap.add_argument("--batch-axes", type=float, nargs=2, default=[0.2, 0.7],
+                    help="--batch: range of the seeded semi-axes")
     ap.add_argument("--sweep-variant", type=int, default=-1,
                     help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
@@ -650,11 +654,12 @@ def run_batch(a):
     from helmholtz_3d_torrone_gb300 import geometry as G
     rng = np.random.default_rng(2024)
     count, wave = a.batch, a.wave
-    grids = [64, 96, 128, 160, 192]
+    grids = list(a.batch_grids)
+    alo, ahi = a.batch_axes
     ops, cases = [], []
     t0 = time.perf_counter()
     for i in range(count):
-        axes = tuple(float(x) for x in rng.uniform(0.2, 0.7, 3))
+        axes = tuple(float(x) for x in rng.uniform(alo, ahi, 3))
         # the 3h tube must keep the WENO stencils off the medial surface:
         # h <= min axis / 7
         need = int(np.ceil(14.0 / min(axes) / 8.0)) * 8
@@ -669,11 +674,11 @@ def run_batch(a):
         cases.append({"axes": [round(x, 4) for x in axes], "N": N, "n_tube": n})
     build_s = time.perf_counter() - t0
     bs = [op.rhs_point_source(np.array([0.02, 0.01, 0.0]), hz.RHS_POINT_DIRICHLET) for op in ops]
-    out = {"mode": "batch", "config": {"workload": "%d ellipsoids, semi-axes U[0.2,0.7] (seed 2024), level sets "
-                                                 "reinitialised on the device, grids 64^3-192^3 over [-1,1]^3, tube "
+    out = {"mode": "batch", "config": {"workload": "%d ellipsoids, semi-axes U[%g,%g] (seed 2024), level sets "
+                                                 "reinitialised on the device, grids %s over [-1,1]^3, tube "
                                                  "|phi|<=3h, k=%g, Dirichlet point source at (0.02,0.01,0)"
-                                                 % (count, wave), "surfaces": cases, "wave": wave,
-                                       "build_s": build_s}}
+                                                 % (count, alo, ahi, "/".join("%d^3" % g for g in grids), wave),
+                                       "surfaces": cases, "wave": wave, "build_s": build_s}}
     with hz.Batch(ops) as b:
         out["config"]["batch_variant"] = b.autotune()[0]
         xs, info, res = b.solve(bs, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)

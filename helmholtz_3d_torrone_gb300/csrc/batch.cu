@@ -10,7 +10,8 @@
 // has converged leaves the batch: the launch is re-described over the
 // operators whose columns still iterate (and the graph captured again), and
 // the refinement neither re-solves it nor recomputes its FP64 residual.  The
-// FP64 products (refinement residuals) run one FP64 sweep per operator.
+// FP64 products (refinement residuals) run one FP64 sweep per operator, the
+// sweeps spread over side streams so that small operators share the GPU.
 #include "hz_internal.cuh"
 #include "krylov.cuh"
 #include "krylov_multi.cuh"
@@ -44,6 +45,16 @@ struct hz_batch {
     size_t partial_bytes = 0;
     KrylovMulti multi;
     DevBuf vec, small;
+    // side streams for the per-operator FP64 products (fork / join on events)
+    std::vector<cudaStream_t> side;
+    std::vector<cudaEvent_t> side_done;
+    cudaEvent_t fork = nullptr;
+    ~hz_batch()
+    {
+        for (cudaStream_t x : side) cudaStreamDestroy(x);
+        for (cudaEvent_t e : side_done) cudaEventDestroy(e);
+        if (fork) cudaEventDestroy(fork);
+    }
 };
 
 namespace {
@@ -88,24 +99,54 @@ struct BatchF32 final : MultiOp {
     }
 };
 
+// The FP64 products (refinement residuals) are one FP64 sweep per
+// operator.  A small operator's sweep fills few SMs, so the sweeps run
+// concurrently on side streams forked from s and joined back to it (each
+// operator has its own density scratch, output column and error word).
+constexpr int kSideStreams = 8;
+
 struct BatchF64 final : MultiOp {
     hz_batch *b;
     std::vector<int> cols;  // empty: every operator
     explicit BatchF64(hz_batch *bb) : b(bb) {}
+    int ensure_side()
+    {
+        if (!b->side.empty()) return HZ_OK;
+        HZ_CHECK_CUDA(cudaEventCreateWithFlags(&b->fork, cudaEventDisableTiming));
+        for (int i = 0; i < kSideStreams; i++) {
+            cudaStream_t x = nullptr;
+            cudaEvent_t e = nullptr;
+            HZ_CHECK_CUDA(cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking));
+            b->side.push_back(x);
+            HZ_CHECK_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+            b->side_done.push_back(e);
+        }
+        return HZ_OK;
+    }
     int apply(int R, const double *p_re, const double *p_im, double *q_re, double *q_im, cudaStream_t s) override
     {
         (void)R;
         HZ_CHECK_CUDA(cudaMemsetAsync(q_re, 0, (size_t)b->R * b->nmax * sizeof(double), s));
         HZ_CHECK_CUDA(cudaMemsetAsync(q_im, 0, (size_t)b->R * b->nmax * sizeof(double), s));
         const int m = cols.empty() ? b->R : (int)cols.size();
-        for (int i = 0; i < m; i++) {
+        HZ_TRY(ensure_side());
+        HZ_CHECK_CUDA(cudaEventRecord(b->fork, s));
+        const int used = m < kSideStreams ? m : kSideStreams;
+        for (int k = 0; k < used; k++) HZ_CHECK_CUDA(cudaStreamWaitEvent(b->side[k], b->fork, 0));
+        int rc = HZ_OK;
+        for (int i = 0; i < m && rc == HZ_OK; i++) {
             const int r = cols.empty() ? i : cols[i];
             hz_operator *op = b->ops[r];
             const size_t off = (size_t)r * b->nmax;
-            HZ_TRY(sweep_f64(sweep_const(op), rec64(op), SWEEP_A, p_re + off, p_im + off, nullptr, nullptr, q_re + off,
-                             q_im + off, nullptr, nullptr, op->scratch.as<double2>(), s));
+            rc = sweep_f64(sweep_const(op), rec64(op), SWEEP_A, p_re + off, p_im + off, nullptr, nullptr, q_re + off,
+                           q_im + off, nullptr, nullptr, op->scratch.as<double2>(), b->side[i % kSideStreams]);
         }
-        return HZ_OK;
+        // join every side stream that was forked, also after a failed launch
+        for (int k = 0; k < used; k++) {
+            HZ_CHECK_CUDA(cudaEventRecord(b->side_done[k], b->side[k]));
+            HZ_CHECK_CUDA(cudaStreamWaitEvent(s, b->side_done[k], 0));
+        }
+        return rc;
     }
     int restrict_to(const std::vector<int> &c, cudaStream_t s) override
     {
