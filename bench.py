@@ -102,6 +102,22 @@ def dist_env():
         os.environ.get("LOCAL_RANK", "0"))
 
 
+def max_over_ranks(dist, seconds, device):
+    """The job's time: the largest of every rank's time (dist None: one rank)."""
+    if dist is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], device=device, dtype=torch.float64)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(pairs_per_step, steps, world, seconds):
+    """Whole-job pair evaluations per second in Gpair/s: every rank (replica)
+    evaluates pairs_per_step pairs per step."""
+    return pairs_per_step * steps * world / seconds / 1e9
+
+
 def workload_desc(N, wave, n):
     return {"workload": "torus R=0.6 r=0.25, phi = analytic signed distance on %d^3 over [-1,1]^3, tube "
                         "|phi|<=3h, k=%g, Dirichlet point source at (0.6,0,0); step = one BiCG iteration "
@@ -275,13 +291,9 @@ def run_gb300(a, rank, world, local):
     launches = hz.kernel_launches() - launches0
     dev_s = ev0.elapsed_time(ev1) / 1e3
     sweep_ms, sweep_launches = op.sweep_timing(-1)
-    elapsed = max(dev_s, 1e-9)
-    if dist is not None:
-        t = torch.tensor([elapsed], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        elapsed = float(t.item())
+    elapsed = max_over_ranks(dist, max(dev_s, 1e-9), dev)
     pairs_step = 2 * n * n
-    value = pairs_step * a.steps * world / elapsed / 1e9
+    value = job_rate(pairs_step, a.steps, world, elapsed)
 
     # ---------------- e2e: host buffers through the C ABI (H2D b, D2H x per step)
     hb_re = torch.from_numpy(np.ascontiguousarray(b.real)).pin_memory()
@@ -298,12 +310,8 @@ def run_gb300(a, rank, world, local):
             flush.fill_(float(_))
         step(hz.HZ_HOST, *hptr)
     torch.cuda.synchronize()
-    e2e_s = time.perf_counter() - t0
-    if dist is not None:
-        t = torch.tensor([e2e_s], device=dev, dtype=torch.float64)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = pairs_step * a.steps * world / e2e_s / 1e9
+    e2e_s = max_over_ranks(dist, time.perf_counter() - t0, dev)
+    e2e = job_rate(pairs_step, a.steps, world, e2e_s)
 
     if rank != 0:
         op.close()
