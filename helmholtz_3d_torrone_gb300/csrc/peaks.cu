@@ -1,8 +1,8 @@
 // peaks.cu -- live FP32 / FP64 FMA throughput of the current GPU.
 //
 // The pair sweeps are bound by the FP32 (and, for the FP64 path, FP64)
-// pipes, whose peaks are not in the measured HBM / bf16 table; this
-// probe measures them the same way on the device the library runs on:
+// pipes.  Measured HBM and bf16 tensor peaks say nothing about these, so
+// this probe measures them on the device the library runs on:
 // independent FMA chains per thread over a grid of 8 blocks per SM.
 #include "hz_internal.cuh"
 

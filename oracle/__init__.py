@@ -333,7 +333,8 @@ class Reference:
 
     def dense_flags(self):
         """POLY_TEST, SINE_TEST, TRAD_ONESIDED, COMBO_ONESIDED, COMBO_INTERIOR,
-        INTERIOR_MODE of this build, and its frame.h sphere (radius, centre)."""
+        INTERIOR_MODE the reference library was compiled with, and its frame.h
+        sphere (radius, centre)."""
         f = np.zeros(6, dtype=np.int32)
         self.L.ref_dense_flags(f.ctypes.data_as(_i32p))
         sph = np.zeros(4)

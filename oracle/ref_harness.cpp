@@ -77,7 +77,7 @@ static void copy_out(double ***g, int S, double *out)
 
 extern "C" {
 
-/* INT_L, INT_U, FACTOR, TAU_FACTOR, DIRICHLET, INTERIOR_MODE of this build. */
+/* INT_L, INT_U, FACTOR, TAU_FACTOR, DIRICHLET, INTERIOR_MODE this library was compiled with. */
 void ref_config(double *out)
 {
     out[0] = INT_L;
