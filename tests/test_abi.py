@@ -83,3 +83,27 @@ def test_bad_params_rejected(hz):
     with pytest.raises(hz.HzError) as e:
         hz.Operator(p)
     assert e.value.code == -1
+
+
+def test_null_handles_and_bad_arguments(hz):
+    """The C entry points answer a NULL handle or a bad argument with
+    HZ_ERR_ARG and a message, before touching a device (the reference would
+    exit(0) or read out of bounds)."""
+    import ctypes as C
+    L = hz.load()
+    opts = hz.solve_opts()
+    info = hz.SolveInfo()
+    cases = {
+        "hz_set_phase_mode": lambda: L.hz_set_phase_mode(None, hz.PHASE_SPLIT),
+        "hz_set_combo": lambda: L.hz_set_combo(None, None),
+        "hz_matvec_multi": lambda: L.hz_matvec_multi(None, hz.PREC_F32, 1, None, None, None, None, hz.HZ_HOST),
+        "hz_solve_multi": lambda: L.hz_solve_multi(None, C.byref(opts), 1, None, None, None, None, hz.HZ_HOST,
+                                                   C.byref(info), None),
+        "hz_batch_create": lambda: L.hz_batch_create(None, 0, C.byref(C.c_void_p())),
+        "hz_batch_solve": lambda: L.hz_batch_solve(None, C.byref(opts), None, None, None, None, hz.HZ_HOST,
+                                                   C.byref(info), None),
+    }
+    for name, call in cases.items():
+        rc = call()
+        assert rc == -1, (name, rc)
+        assert L.hz_last_error().decode(), name
