@@ -100,6 +100,8 @@ class Oracle:
                               C.c_int, C.c_int]
         L.or_point_source_rhs.argtypes = [P, C.c_int64, _dp, _dp, _dp, C.c_int, _dp, _dp]
         L.or_reinit.argtypes = [C.c_int, C.c_double, _dp, C.c_int, C.c_double, C.c_int]
+        L.or_godunov.argtypes = [C.c_double] * 7
+        L.or_godunov.restype = C.c_double
         D = C.POINTER(DenseOpts)
         L.or_dense_points.argtypes = [C.c_int, P, D] + [_dp] * 6 + [C.c_int64, _dp]
         L.or_dense_points.restype = C.c_int64
@@ -115,6 +117,9 @@ class Oracle:
         p, n = C.c_double(), C.c_double()
         self.L.or_weno(C.byref(p), C.byref(n), _d(fi), dx, order)
         return p.value, n.value
+
+    def godunov(self, signage, a, b, c, d, e, f):
+        return self.L.or_godunov(signage, a, b, c, d, e, f)
 
     def gradient(self, N, H, d, order=5):
         d = np.ascontiguousarray(d, dtype=np.float64)
@@ -263,6 +268,8 @@ class Reference:
         L.ref_h.restype = C.c_double
         L.ref_eps.restype = C.c_double
         L.ref_weno.argtypes = [_dp, _dp, _dp, C.c_double, C.c_int]
+        L.ref_godunov.argtypes = [C.c_double] * 7
+        L.ref_godunov.restype = C.c_double
         L.ref_tube.argtypes = [C.c_double, _ip]
         L.ref_tube.restype = C.c_int64
         L.ref_tube_points.argtypes = [C.c_double, C.c_int64] + [_dp] * 6
@@ -303,6 +310,9 @@ class Reference:
         p, n = C.c_double(), C.c_double()
         self.L.ref_weno(C.byref(p), C.byref(n), _d(fi), dx, order)
         return p.value, n.value
+
+    def godunov(self, signage, a, b, c, d, e, f):
+        return self.L.ref_godunov(signage, a, b, c, d, e, f)
 
     def tube(self):
         eps = self.L.ref_eps()

@@ -179,6 +179,11 @@ static double godunov(double signage, double a, double b, double c, double d, do
     return 0.0;
 }
 
+double or_godunov(double signage, double a, double b, double c, double d, double e, double f)
+{
+    return godunov(signage, a, b, c, d, e, f);
+}
+
 /* One stage of phi_t + S(phi0)(|grad phi| - 1) = 0 (see or_reinit). */
 static void reinit_stage(int N, double H, double dt, const double *phi0, const double *phi, const double *base,
                          double w0, double w1, double *out, int order)

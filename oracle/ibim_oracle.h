@@ -62,6 +62,9 @@ void or_curvatures(int N, double H, const double *d, double *mcurv, double *gcur
  * unused Godunov(), finite_difference3D.c:5-27): iters TVD-RK2 steps of
  * phi_t + S(phi0)(|grad phi| - 1) = 0, S = phi0/sqrt(phi0^2+H^2), WENO
  * one-sided derivatives, dt = cfl*H.  In place. */
+/* Godunov upwind |grad phi| of one node from its six one-sided
+ * derivatives (finite_difference3D.c:5-27). */
+double or_godunov(double signage, double a, double b, double c, double d, double e, double f);
 void or_reinit(int N, double H, double *phi, int iters, double cfl, int order);
 
 /* Tube {|d| <= eps} in lexicographic (i,j,k) order, large3Dexample2.c:548-597.

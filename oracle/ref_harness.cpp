@@ -31,6 +31,7 @@ int ASSIGN_GRADIENT(int N, double H, double ***dist, double ***graddx, double **
 int BothCurvs(double ***dist, int i, int j, int k, int N, double H, double *meancurv,
               double *gausscurv);
 void weno(double *dfp, double *dfn, double fi[], const double dx, const int order);
+double Godunov(double signage, double a, double b, double c, double d, double e, double f);
 int cal_interpgrad(int N, double H, double xj, double yj, double zj, double ***gradx,
                    double ***grady, double ***gradz, double *interpolatex, double *interpolatey,
                    double *interpolatez);
@@ -131,6 +132,12 @@ void ref_weno(double *dfp, double *dfn, const double *fi, double dx, int order)
     double f[7];
     memcpy(f, fi, (order == 5 ? 7 : 5) * sizeof(double));
     weno(dfp, dfn, f, dx, order);
+}
+
+/* finite_difference3D.c:5-27, as compiled here. */
+double ref_godunov(double signage, double a, double b, double c, double d, double e, double f)
+{
+    return Godunov(signage, a, b, c, d, e, f);
 }
 
 /* main :548-597: members |d| <= eps in (i,j,k) order, as linear indices. */

@@ -10,7 +10,8 @@ entries, the dense products A p and A^H p for a seeded p, and the CompBiCG
 density for a point-source right-hand side solved to 1e-13.  The dense
 case holds the per-point arrays of the three dense assemblers of
 HelmholtzKernel.c, a sample of their matrix entries and their products with
-a seeded vector.
+a seeded vector.  The Godunov case holds the reference's upwind |grad phi|
+(finite_difference3D.c:5-27) for seeded one-sided derivatives.
 
 Usage:  python oracle/build_ref.py && python tests/golden/make_golden.py
 """
@@ -161,10 +162,29 @@ def run_dense_case(name):
     return name, n_dl
 
 
+# Godunov upwind |grad phi| (finite_difference3D.c:5-27), the Hamiltonian
+# of the level-set reinitialisation: seeded one-sided derivatives with
+# zeros and both signs mixed in, for signage -1, 0 and +1.
+GODUNOV_CASES = {"ref_godunov": dict(variant="neumann", count=1500, seed=5)}
+
+
+def run_godunov_case(name):
+    import oracle as O
+    case = GODUNOV_CASES[name]
+    ref = O.Reference(case["variant"])
+    rng = np.random.default_rng(case["seed"])
+    x = rng.standard_normal((case["count"], 6))
+    x[rng.random(x.shape) < 0.15] = 0.0
+    sig = rng.choice([-1.0, 0.0, 1.0], size=case["count"])
+    out = np.array([ref.godunov(s, *row) for s, row in zip(sig, x)])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), signage=sig, derivs=x, out=out)
+    return name
+
+
 def main():
     # One process per case: the reference exits (status 0) on some inputs and
     # keeps per-process statics, so each case gets a fresh, time-limited child.
-    names = sys.argv[1:] or list(CASES) + list(DENSE_CASES)
+    names = sys.argv[1:] or list(CASES) + list(DENSE_CASES) + list(GODUNOV_CASES)
     for name in names:
         out = os.path.join(HERE, name + ".npz")
         if os.path.exists(out):
@@ -181,6 +201,8 @@ if __name__ == "__main__":
     if len(sys.argv) == 3 and sys.argv[1] == "--one":
         if sys.argv[2] in DENSE_CASES:
             run_dense_case(sys.argv[2])
+        elif sys.argv[2] in GODUNOV_CASES:
+            run_godunov_case(sys.argv[2])
         else:
             run_case(sys.argv[2])
     else:

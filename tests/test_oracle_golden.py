@@ -74,3 +74,13 @@ def test_weno_bitexact(oracle):
     fi = g["weno_in"]
     out = [oracle.weno(f, 0.1, 5) for f in fi] + [oracle.weno(f[:5], 0.1, 3) for f in fi]
     assert np.array_equal(np.array(out), g["weno_out"])
+
+
+def test_godunov_bitexact(oracle):
+    """The oracle's Godunov upwind |grad phi| (the reinitialisation's
+    Hamiltonian) equals the reference's finite_difference3D.c:5-27 bit for
+    bit on the seeded fixture (zeros, both signs, signage -1 / 0 / +1)."""
+    g = golden("ref_godunov")
+    out = np.array([oracle.godunov(s, *row) for s, row in zip(g["signage"], g["derivs"])])
+    assert np.array_equal(out, g["out"])
+    assert np.count_nonzero(g["out"]) > 0.5 * g["out"].size
