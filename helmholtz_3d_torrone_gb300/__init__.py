@@ -33,26 +33,36 @@ ERRORS = {-1: "HZ_ERR_ARG", -2: "HZ_ERR_CUDA", -3: "HZ_ERR_STATE", -4: "HZ_ERR_G
 
 
 class HzError(RuntimeError):
+    """A failed C call: .code is the HZ_ERR_* status, the message hz_last_error()."""
     def __init__(self, code, msg):
         super().__init__("%s (%d): %s" % (ERRORS.get(code, "?"), code, msg))
         self.code = code
 
 
 class Params(C.Structure):
+    """hz_params: grid size N over [int_l, int_u]^3, wave number, tube factor
+    (eps = factor H), near-field factor (tau = tau_factor H), formulation
+    (dirichlet, interior) and WENO order; build one with params()."""
     _fields_ = [("N", C.c_int), ("int_l", C.c_double), ("int_u", C.c_double), ("wave", C.c_double),
                 ("factor", C.c_double), ("tau_factor", C.c_double), ("dirichlet", C.c_int),
                 ("interior", C.c_int), ("weno_order", C.c_int)]
 
     @property
     def H(self):
+        """Grid spacing (int_u - int_l) / N (large3Dexample2.c:174)."""
         return (self.int_u - self.int_l) / self.N
 
     @property
     def eps(self):
+        """Tube half-width factor * H."""
         return self.factor * self.H
 
 
 class SolveOpts(C.Structure):
+    """hz_solve_opts: method (BICG, BICGSTAB, GMRES), precision (PREC_F64,
+    PREC_F32, PREC_F32_REFINED), tolerance, iteration limits, inner
+    tolerance and refinement steps of PREC_F32_REFINED, stagnation stop,
+    GMRES restart length; build one with solve_opts()."""
     _fields_ = [("method", C.c_int), ("precision", C.c_int), ("tol", C.c_double), ("maxit", C.c_int),
                 ("inner_tol", C.c_double), ("max_outer", C.c_int), ("stagnation", C.c_int), ("restart", C.c_int)]
 
@@ -73,10 +83,14 @@ class RefConfig(C.Structure):
 
 
 class SolveInfo(C.Structure):
+    """hz_solve_info: iterations (inner ones for refined solves), refinement
+    steps, final relative residual (FP64 for refined solves), seconds, pair
+    evaluations and status."""
     _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("resid", C.c_double), ("resid_f64", C.c_double),
                 ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int)]
 
     def as_dict(self):
+        """The fields as a dict."""
         return {f: getattr(self, f) for f, _ in self._fields_}
 
 
@@ -198,10 +212,13 @@ def params(N, wave, int_l=-2.0, int_u=2.0, factor=2.0, tau_factor=2.0, dirichlet
 
 def solve_opts(method=BICG, precision=PREC_F64, tol=1e-7, maxit=2000, inner_tol=1e-5, max_outer=20,
                stagnation=1, restart=40):
+    """SolveOpts with the C defaults (hz_solve_opts_default) unless given."""
     return SolveOpts(method, precision, tol, maxit, inner_tol, max_outer, stagnation, restart)
 
 
 def kernel_launches():
+    """Kernels this library has launched so far (graph replays counted by
+    their nodes)."""
     return int(load().hz_kernel_launches())
 
 
@@ -224,6 +241,7 @@ class Operator:
         self.n = None
 
     def close(self):
+        """Release the device memory (also on garbage collection)."""
         if getattr(self, "h", None):
             load().hz_destroy(self.h)
             self.h = None
@@ -241,6 +259,7 @@ class Operator:
         self.close()
 
     def set_stream(self, stream_handle):
+        """Run the operator's work on this CUDA stream (a cudaStream_t as int)."""
         _check(load().hz_set_stream(self.h, stream_handle))
 
     def shape_gradient(self, src, receivers, target, opts=None, **kw):
@@ -263,6 +282,7 @@ class Operator:
         _check(load().hz_set_combo(self.h, None if opts is None else C.byref(opts)))
 
     def set_distance(self, d, where=HZ_HOST):
+        """The signed-distance grid, (N+1)^3 values, node (i, j, k) at [i, j, k]."""
         if where == HZ_HOST:
             d = _f64(d)
             S = self.p.N + 1
@@ -271,6 +291,8 @@ class Operator:
         _check(load().hz_set_distance(self.h, _ptr(d), where))
 
     def build(self):
+        """Stencil grids, tube, projected points, weights and sweep records;
+        returns the tube size n."""
         n = C.c_int64()
         _check(load().hz_build(self.h, C.byref(n)))
         self.n = n.value
@@ -283,6 +305,7 @@ class Operator:
         return cfg.value, ms.value
 
     def set_sweep_config(self, cfg):
+        """Force FP32 sweep variant cfg (0 .. 7) instead of the autotuned one."""
         _check(load().hz_set_sweep_config(self.h, cfg))
 
     def set_phase_mode(self, mode):
@@ -297,12 +320,15 @@ class Operator:
         return ms.value, k.value
 
     def grids(self):
+        """[gx, gy, gz, mean curvature, Gaussian curvature] on the grid."""
         S = self.p.N + 1
         g = [np.empty((S, S, S)) for _ in range(5)]
         _check(load().hz_get_grids(self.h, *[_ptr(a) for a in g], HZ_HOST))
         return g
 
     def tube(self):
+        """Tube points in the reference's order: node idx, x*, normals, delta,
+        Jacobian, regularisation factor and weight."""
         n = self.n
         idx = np.empty(n, dtype=np.int64)
         xs, nrm = np.empty((n, 3)), np.empty((n, 3))
@@ -312,18 +338,22 @@ class Operator:
         return dict(idx=idx, xs=xs, nrm=nrm, delta=delta, jac=jac, reg=reg, w=w)
 
     def matvec(self, v, precision=PREC_F64, adjoint=False):
+        """A v (or A^H v) in FP64 or FP32."""
         vr, vi = _f64(v.real), _f64(v.imag)
         qr, qi = np.empty(self.n), np.empty(self.n)
         _check(load().hz_matvec(self.h, precision, int(adjoint), _ptr(vr), _ptr(vi), _ptr(qr), _ptr(qi), HZ_HOST))
         return qr + 1j * qi
 
     def matvec_pair(self, v, vt, precision=PREC_F64):
+        """(A v, A^H vt) in one fused pass over the pairs."""
         a = [_f64(v.real), _f64(v.imag), _f64(vt.real), _f64(vt.imag)]
         q = [np.empty(self.n) for _ in range(4)]
         _check(load().hz_matvec_pair(self.h, precision, *[_ptr(x) for x in a], *[_ptr(x) for x in q], HZ_HOST))
         return q[0] + 1j * q[1], q[2] + 1j * q[3]
 
     def matvec_multi(self, V, precision=PREC_F32):
+        """A V for every row of V ([nrhs][n]), one pair evaluation per pass
+        over a block of rows."""
         V = np.atleast_2d(V)
         nrhs = V.shape[0]
         vr, vi = _f64(V.real), _f64(V.imag)
@@ -332,6 +362,8 @@ class Operator:
         return qr + 1j * qi
 
     def solve(self, b, opts=None, **kw):
+        """Solve A x = b; returns (x, info dict).  opts: SolveOpts, else
+        solve_opts(**kw)."""
         opts = opts if opts is not None else solve_opts(**kw)
         br, bi = _f64(b.real), _f64(b.imag)
         xr, xi = np.empty(self.n), np.empty(self.n)
@@ -354,6 +386,8 @@ class Operator:
         return xr + 1j * xi, info.as_dict(), res
 
     def rhs_plane_waves(self, dirs, kind=RHS_POINT_DIRICHLET):
+        """Boundary data of incident plane waves e^{ik d.x}, one row per
+        direction in dirs."""
         d = _f64(dirs).reshape(-1, 3)
         m = d.shape[0]
         br, bi = np.empty((m, self.n)), np.empty((m, self.n))
@@ -388,12 +422,15 @@ class Operator:
         return J.value, gr + 1j * gi, dk.value, gw, info.as_dict()
 
     def rhs_point_source(self, src, kind):
+        """Boundary data of a point source at src (RHS_* kind)."""
         s = _f64(src)
         br, bi = np.empty(self.n), np.empty(self.n)
         _check(load().hz_rhs_point_source(self.h, _ptr(s), kind, _ptr(br), _ptr(bi), HZ_HOST))
         return br + 1j * bi
 
     def evaluate(self, receivers, sigma, layer):
+        """Field of the density sigma at receivers ([m][3]) for the layer
+        (SINGLE_LAYER, DOUBLE_LAYER or COMBO_LAYER)."""
         rx = _f64(receivers).reshape(-1, 3)
         m = rx.shape[0]
         sr, si = _f64(sigma.real), _f64(sigma.imag)
@@ -450,6 +487,7 @@ class Batch:
         self.h = h
 
     def close(self):
+        """Destroy the batch (the operators stay)."""
         if self.h:
             load().hz_batch_destroy(self.h)
             self.h = None
@@ -461,11 +499,14 @@ class Batch:
         self.close()
 
     def autotune(self):
+        """Time the batch sweep shapes on this batch and keep the fastest:
+        (shape, ms per product)."""
         cfg, ms = C.c_int(), C.c_double()
         _check(load().hz_batch_autotune(self.h, C.byref(cfg), C.byref(ms)))
         return cfg.value, ms.value
 
     def set_variant(self, v):
+        """Force batch sweep shape v (0 .. 3)."""
         _check(load().hz_batch_set_variant(self.h, v))
 
     @staticmethod
@@ -473,6 +514,7 @@ class Batch:
         return (_vp * len(arrs))(*[a.ctypes.data for a in arrs])
 
     def matvec(self, vs, precision=PREC_F32):
+        """A_r v_r for every operator r of the batch."""
         pr = [_f64(v.real) for v in vs]
         pi = [_f64(v.imag) for v in vs]
         qr = [np.empty(o.n) for o in self.ops]
@@ -482,6 +524,8 @@ class Batch:
         return [a + 1j * b for a, b in zip(qr, qi)]
 
     def solve(self, bs, opts=None, **kw):
+        """Solve every A_r x_r = b_r together; returns (xs, info dict,
+        residuals)."""
         opts = opts if opts is not None else solve_opts(**kw)
         br = [_f64(b.real) for b in bs]
         bi = [_f64(b.imag) for b in bs]
@@ -563,39 +607,46 @@ def reference_file_names(N, wave):
 
 
 def read_distance_file(path, N):
+    """A distance<N>.txt grid in the reference's format ((N+1)^3 values)."""
     d = np.empty((N + 1,) * 3)
     _check(load().hz_read_distance_file(path.encode(), N, _ptr(d)))
     return d
 
 
 def write_distance_file(path, N, d):
+    """Write a grid in the reference's distance-file format."""
     d = _f64(d)
     _check(load().hz_write_distance_file(path.encode(), N, _ptr(d)))
 
 
 def write_rhs_files(path_re, path_im, b):
+    """Boundary data in the reference's b / bimg file format."""
     br, bi = _f64(b.real), _f64(b.imag)
     _check(load().hz_write_rhs_files(path_re.encode(), path_im.encode(), len(br), _ptr(br), _ptr(bi)))
 
 
 def read_rhs_files(path_re, path_im, n):
+    """Read n complex boundary values from the reference's b / bimg files."""
     br, bi = np.empty(n), np.empty(n)
     _check(load().hz_read_rhs_files(path_re.encode(), path_im.encode(), n, _ptr(br), _ptr(bi)))
     return br + 1j * bi
 
 
 def write_density_files(path_re, path_im, x):
+    """A density in the reference's density / densityimg file format."""
     xr, xi = _f64(x.real), _f64(x.imag)
     _check(load().hz_write_density_files(path_re.encode(), path_im.encode(), len(xr), _ptr(xr), _ptr(xi)))
 
 
 def read_density_files(path_re, path_im, n):
+    """Read n complex density values from the reference's density files."""
     xr, xi = np.empty(n), np.empty(n)
     _check(load().hz_read_density_files(path_re.encode(), path_im.encode(), n, _ptr(xr), _ptr(xi)))
     return xr + 1j * xi
 
 
 def write_result_file(path, exact, approx):
+    """Append one line of the reference's Rel_Result log (exact and computed field)."""
     _check(load().hz_write_result_file(path.encode(), exact.real, exact.imag, approx.real, approx.imag))
 
 
