@@ -30,6 +30,7 @@ NOALLOC_MAX_POINTS = 32768  # HZ_NOALLOC_MAX_POINTS
 
 ERRORS = {-1: "HZ_ERR_ARG", -2: "HZ_ERR_CUDA", -3: "HZ_ERR_STATE", -4: "HZ_ERR_GRID",
           -5: "HZ_ERR_NONFINITE", -6: "HZ_ERR_BREAKDOWN", -7: "HZ_ERR_DEVICE_WAIT"}
+globals().update({name: code for code, name in ERRORS.items()})
 
 
 class HzError(RuntimeError):
@@ -79,15 +80,16 @@ class RefConfig(C.Structure):
     dense assemblers read (include/helmholtz_ref_api.h)."""
     _fields_ = [("int_l", C.c_double), ("int_u", C.c_double), ("tau_factor", C.c_double), ("interior", C.c_int),
                 ("poly", C.c_int), ("sine", C.c_int), ("trad_onesided", C.c_int), ("combo_onesided", C.c_int),
-                ("combo_interior", C.c_int), ("radius", C.c_double), ("center", C.c_double * 3)]
+                ("combo_interior", C.c_int), ("radius", C.c_double), ("center", C.c_double * 3),
+                ("bicg_acc", C.c_double)]
 
 
 class SolveInfo(C.Structure):
     """hz_solve_info: iterations (inner ones for refined solves), refinement
     steps, final relative residual (FP64 for refined solves), seconds, pair
-    evaluations and status."""
+    evaluations, status and whether the final residual is below tol."""
     _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("resid", C.c_double), ("resid_f64", C.c_double),
-                ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int)]
+                ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int), ("converged", C.c_int)]
 
     def as_dict(self):
         """The fields as a dict."""
@@ -151,6 +153,7 @@ SIGNATURES = {
     "hz_ref_get_config": ([C.POINTER(RefConfig)], None),
     "hz_ref_set_config": ([C.POINTER(RefConfig)], None),
     "hz_kernel_launches": ([], C.c_int64),
+    "hz_set_wait_limit": ([C.c_longlong], C.c_int),
     "hz_measure_fma_peaks": ([_dp, _dp], C.c_int),
     "hz_eval_slice": ([_vp, C.c_int, C.c_int, C.c_double, C.c_int, C.c_double, C.c_double, C.c_double, _vp, _vp,
                        _vp, _vp, C.c_int], C.c_int),
@@ -220,6 +223,13 @@ def kernel_launches():
     """Kernels this library has launched so far (graph replays counted by
     their nodes)."""
     return int(load().hz_kernel_launches())
+
+
+def set_wait_limit(polls=-1):
+    """Poll limit of the pair sweeps' data waits on the current device
+    (negative: the default).  A short limit makes the waits give up, which
+    the sweeps report as HZ_ERR_DEVICE_WAIT."""
+    _check(load().hz_set_wait_limit(int(polls)))
 
 
 def measure_fma_peaks():

@@ -2,7 +2,9 @@
 
 Translation units are compiled in parallel, one ``-gencode`` each.  The
 stencil and tube units use ``-fmad=false`` so the level-set preprocessing
-keeps the reference's unfused FP64 operation order (bit-identical grids);
+keeps the reference's unfused FP64 operation order (bit-identical grids;
+the stencil unit's host code, the per-node entry points, is built with
+``-ffp-contract=off`` for the same reason);
 the pair sweeps and solvers use fused multiply-adds.
 """
 import os
@@ -20,7 +22,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "--extended-lambda", "-Xcompiler", "-fPIC",
           "-Xcompiler", "-fvisibility=hidden", "-I", CSRC]
 UNITS = {
-    "stencils.cu": ["-fmad=false"],
+    "stencils.cu": ["-fmad=false", "-Xcompiler", "-ffp-contract=off"],
     "tube.cu": ["-fmad=false"],
     "dense.cu": ["-fmad=false"],
     "sweep_f64.cu": [],

@@ -458,6 +458,7 @@ int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts_in, const double *cons
     inf.pair_evals = pairs;
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     inf.status = rc;
+    inf.converged = w < o.tol ? 1 : 0;
     if (info) *info = inf;
     return rc;
 }

@@ -3,7 +3,7 @@
 //
 // Rules kept by every caller: global source and shared destination are
 // 16-byte aligned and every copy size is a multiple of 16 bytes.  Every wait
-// polls at most kWaitLimit times; on timeout it reports failure instead of
+// polls a bounded number of times; on timeout it reports failure instead of
 // spinning forever, so a lost copy turns into an error status, not a hang.
 #pragma once
 
@@ -62,5 +62,29 @@ __device__ __forceinline__ bool mbar_wait_bounded(uint64_t *bar, uint32_t parity
         if (mbar_try_wait(bar, parity)) return true;
     return false;
 }
+
+// Poll limit of the data waits (a CTA waiting for its next source tile).
+// Each translation unit that includes this header holds its own copy on
+// every device; hz_set_wait_limit sets them all on the current device (a
+// short limit makes the waits give up, for tests of the error path).
+static __device__ long long g_data_wait_limit = 1ll << 24;
+
+// After a data wait gave up: the copies this CTA still has in flight (the
+// buffer waited on and, when it was issued, the other one) must land before
+// the CTA exits and its shared memory is reused.  Called by the thread that
+// issued them; these waits keep the full bound whatever the data-wait limit.
+__device__ __forceinline__ void mbar_drain(uint64_t *cur, uint32_t pcur, uint64_t *other, uint32_t pother,
+                                           bool other_issued)
+{
+    mbar_wait_bounded(cur, pcur, 1ll << 24);
+    if (other_issued) mbar_wait_bounded(other, pother, 1ll << 24);
+}
+
+// Host side: set this translation unit's copy of the limit on the current device.
+#define HZ_DEFINE_WAIT_LIMIT_SETTER(name)                                                        \
+    int name(long long polls)                                                                    \
+    {                                                                                            \
+        return cudaMemcpyToSymbol(g_data_wait_limit, &polls, sizeof(polls)) == cudaSuccess ? 0 : -1; \
+    }
 
 }  // namespace hz

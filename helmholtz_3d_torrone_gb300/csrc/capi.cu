@@ -288,6 +288,7 @@ struct hz_solver_state {
     DevBuf small;
     DevBuf mvec, mscratch, mpack;  // multi right-hand side staging, sweep scratch, packed columns
     DevBuf gwork, gsmall, gx;  // GMRES basis, Hessenberg partials, inner solution
+    DevBuf xbest;              // refinement: best iterate so far (re/im)
 };
 
 namespace {
@@ -461,6 +462,18 @@ int hz_set_combo(hz_operator *op, const hz_dense_opts *o)
 }
 
 int64_t hz_kernel_launches(void) { return g_launches.load(); }
+
+int hz_set_wait_limit(long long polls)
+{
+    if (polls < 0) polls = kWaitLimit;
+    if (set_wait_limit_f32(polls) || set_wait_limit_combo32(polls) || set_wait_limit_f64(polls) ||
+        set_wait_limit_multi(polls)) {
+        set_error("hz_set_wait_limit: cudaMemcpyToSymbol failed");
+        cudaGetLastError();
+        return HZ_ERR_CUDA;
+    }
+    return HZ_OK;
+}
 
 void hz_params_default(hz_params *p, int N, double wave)
 {
@@ -971,6 +984,7 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
     inf.pair_evals = pairs;
     inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
     inf.status = rc;
+    inf.converged = worst < o.tol ? 1 : 0;
     if (info) *info = inf;
     return rc;
 }
@@ -1021,6 +1035,20 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
     int iters = 0;
     status = HZ_OK;
     double resid = 0.0;
+    {
+        // a NaN or Inf in b would read as "no data" (x = 0) to the Krylov
+        // start test; the reference exits on it (large3Dexample2.c:2641)
+        double nb = 0.0;
+        double *part = st->small.as<double>();
+        HZ_TRY(vec_norm(n, b0, b1, part, part + (vec_partial_bytes() / sizeof(double)), nb, s));
+        if (!std::isfinite(nb)) {
+            HZ_CHECK_CUDA(cudaMemsetAsync(x0, 0, n * sizeof(double), s));
+            HZ_CHECK_CUDA(cudaMemsetAsync(x1, 0, n * sizeof(double), s));
+            status = HZ_ERR_NONFINITE;
+            inf.converged = 0;
+            return HZ_OK;
+        }
+    }
     if (o.precision != HZ_PREC_F32_REFINED && o.method == HZ_GMRES) {
         MatrixFreeOp Af(op, o.precision);
         AdjointOp Aa(Af);
@@ -1032,6 +1060,7 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         inf.resid = resid;
         inf.resid_f64 = (o.precision == HZ_PREC_F64) ? resid : -1.0;
         inf.pair_evals = (long long)products * n * n;
+        inf.converged = resid < o.tol ? 1 : 0;
         return HZ_OK;
     }
     if (o.precision != HZ_PREC_F32_REFINED) {
@@ -1047,6 +1076,7 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         inf.resid_f64 = (o.precision == HZ_PREC_F64) ? resid : -1.0;
         // two matrix products per iteration (A p and A^H pt, or two A products)
         inf.pair_evals = 2LL * iters * n * n;
+        inf.converged = resid < o.tol ? 1 : 0;
         return HZ_OK;
     }
     // FP64 iterative refinement around FP32 inner solves.
@@ -1069,6 +1099,12 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
     long long products = 0;
     const bool gm = o.method == HZ_GMRES;
     if (gm) HZ_TRY(st->gx.ensure((size_t)n * 2 * sizeof(double)));
+    // the best iterate (lowest FP64 residual) is kept: a step that does not
+    // lower the residual ends the refinement and the best iterate is returned
+    HZ_TRY(st->xbest.ensure((size_t)n * 2 * sizeof(double)));
+    double *xb0 = st->xbest.as<double>(), *xb1 = xb0 + n;
+    double best = res;
+    bool stalled = false;
     while (normb > 0 && res >= o.tol && outer < o.max_outer) {
         outer++;
         // inner right-hand side r / ||r|| (into q)
@@ -1102,17 +1138,32 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         HZ_TRY(vec_sub(n, b0, b1, q0, q1, r0, r1, s));
         HZ_TRY(vec_norm(n, r0, r1, part, dout, nr, s));
         A64.iteration_done(false);
-        const double prev = res;
         res = nr / normb;
-        if (ist == HZ_ERR_BREAKDOWN && !(res < prev)) {
-            status = HZ_ERR_BREAKDOWN;
+        if (!(res < best)) {
+            // no progress (or a non-finite residual): back to the best iterate
+            if (outer > 1) {
+                HZ_CHECK_CUDA(cudaMemcpyAsync(x0, xb0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+                HZ_CHECK_CUDA(cudaMemcpyAsync(x1, xb1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            } else {
+                HZ_CHECK_CUDA(cudaMemsetAsync(x0, 0, n * sizeof(double), s));
+                HZ_CHECK_CUDA(cudaMemsetAsync(x1, 0, n * sizeof(double), s));
+            }
+            res = best;
+            stalled = true;
+            if (ist == HZ_ERR_BREAKDOWN) status = HZ_ERR_BREAKDOWN;
             break;
+        }
+        best = res;
+        if (res >= o.tol && outer < o.max_outer) {
+            HZ_CHECK_CUDA(cudaMemcpyAsync(xb0, x0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            HZ_CHECK_CUDA(cudaMemcpyAsync(xb1, x1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         }
     }
     inf.iterations = iters;
     inf.outer = outer;
     inf.resid = res;
     inf.resid_f64 = res;
+    inf.converged = (!stalled && res < o.tol) ? 1 : 0;
     // inner products (two per BiCG iteration); one FP64 residual product per step
     inf.pair_evals = (products + outer) * (long long)n * n;
     return HZ_OK;
@@ -1167,7 +1218,9 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
     if (info) *info = inf;
     if (rc != HZ_OK) return rc;
     if (status != HZ_OK) {
-        set_error("solver stopped early (status %d)", status);
+        if (status == HZ_ERR_NONFINITE) set_error("hz_solve: non-finite value in the right-hand side or an iterate");
+        else if (status == HZ_ERR_BREAKDOWN) set_error("hz_solve: Krylov breakdown (a zero denominator)");
+        else set_error("hz_solve: solver stopped early (status %d)", status);
         return status;
     }
     return HZ_OK;
@@ -1271,6 +1324,7 @@ int hz_misfit_gradient(hz_operator *op, const hz_solve_opts *opts_in, const doub
         inf.pair_evals = fwd.pair_evals + adj.pair_evals + n * n;
         inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         inf.status = rc != HZ_OK ? rc : (status != HZ_OK ? status : status2);
+        inf.converged = (fwd.converged && adj.converged) ? 1 : 0;
         *info = inf;
     }
     if (rc != HZ_OK) return rc;
@@ -1346,6 +1400,7 @@ int hz_shape_gradient(hz_operator *op, const hz_solve_opts *opts_in, const doubl
         inf.pair_evals = fwd.pair_evals + adj.pair_evals + n * n;
         inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         inf.status = rc != HZ_OK ? rc : (status != HZ_OK ? status : status2);
+        inf.converged = (fwd.converged && adj.converged) ? 1 : 0;
         *info = inf;
     }
     if (rc != HZ_OK) return rc;
@@ -1577,6 +1632,7 @@ int hz_dense_bicg(int64_t n, const double *a_re, const double *a_im, const doubl
         inf.resid = resid;
         inf.resid_f64 = resid;
         inf.status = status;
+        inf.converged = resid < tol ? 1 : 0;
         inf.seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
         *info = inf;
     }

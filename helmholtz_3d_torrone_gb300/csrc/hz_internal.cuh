@@ -198,6 +198,12 @@ int sweep_order(int N, int64_t n, const int64_t *idx, int *perm, int64_t npad, D
 int build_rec32(const Rec32 &r, const double4_32a *pos64, const double4_32a *nrm64, double reg_scale, double tau,
                 cudaStream_t s);
 // sweep_f64.cu
+// Data-wait poll limit of each sweep translation unit, on the current device.
+int set_wait_limit_f32(long long polls);
+int set_wait_limit_combo32(long long polls);
+int set_wait_limit_f64(long long polls);
+int set_wait_limit_multi(long long polls);
+
 int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re, const double *p_im,
               const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
               double *qt_im, double2 *scratch, cudaStream_t s, cudaEvent_t ev0 = nullptr,

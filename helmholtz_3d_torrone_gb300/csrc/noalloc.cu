@@ -26,32 +26,76 @@ constexpr size_t kStaticBytes = 3 * kRecBytes + 256;  // pos, nrm, densities, er
 // its device address comes from cudaGetSymbolAddress.
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kStaticBytes];
 
-constexpr int kMaxDevices = 64;
+// Device addresses of the scratch, one per CUDA context: a __device__
+// symbol's address belongs to the context that loaded the module, not to the
+// device, so a context of the caller's own (cuCtxCreate / cuCtxSetCurrent) or
+// a new primary context after cudaDeviceReset has its own copy.
+constexpr int kMaxContexts = 64;
 std::mutex g_mu;
-void *g_addr[kMaxDevices] = {};
+struct CtxAddr {
+    void *ctx;
+    void *addr;
+};
+CtxAddr g_addr[kMaxContexts] = {};
+int g_used = 0;
 
-// Device address of the scratch for the current device, looked up once per
-// device (the first call on a device does this with that device current).
-int scratch_address(void **out)
+typedef int (*CtxGetCurrentFn)(void **);
+
+// The driver's cuCtxGetCurrent, reached through the runtime so that the
+// library needs no link against libcuda.
+void *current_context()
 {
-    int dev = 0;
-    HZ_CHECK_CUDA(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kMaxDevices) {
-        set_error("hz_matvec_f64_noalloc: device ordinal %d out of range", dev);
-        return HZ_ERR_ARG;
-    }
+    static CtxGetCurrentFn fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void *f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<CtxGetCurrentFn>(f);
+        cudaGetLastError();
+    });
+    void *ctx = nullptr;
+    if (!fn || fn(&ctx) != 0) return nullptr;
+    return ctx;
+}
+
+// Device address of the scratch in the current context.  Outside stream
+// capture the address is looked up again on every call (a host-side lookup,
+// no device work), so a reset device or a switched context never sees a
+// stale address; while `s` is capturing, the address cached for the current
+// context by an earlier call is used, so the first call in a context must
+// come before any capture.
+int scratch_address(cudaStream_t s, void **out)
+{
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    HZ_CHECK_CUDA(cudaStreamIsCapturing(s, &cap));
+    void *ctx = current_context();
     std::lock_guard<std::mutex> lock(g_mu);
-    if (!g_addr[dev]) {
-        void *p = nullptr;
-        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-        if (e != cudaSuccess || !p) {
-            set_error("hz_matvec_f64_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
-            cudaGetLastError();
-            return HZ_ERR_CUDA;
+    int slot = -1;
+    for (int i = 0; i < g_used; i++)
+        if (g_addr[i].ctx == ctx) slot = i;
+    if (cap != cudaStreamCaptureStatusNone) {
+        if (slot < 0 || !g_addr[slot].addr) {
+            set_error("hz_matvec_f64_noalloc: first call in this CUDA context made during stream capture");
+            return HZ_ERR_STATE;
         }
-        g_addr[dev] = p;
+        *out = g_addr[slot].addr;
+        return HZ_OK;
     }
-    *out = g_addr[dev];
+    void *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+    if (e != cudaSuccess || !p) {
+        set_error("hz_matvec_f64_noalloc: cudaGetSymbolAddress failed: %s", cudaGetErrorString(e));
+        cudaGetLastError();
+        return HZ_ERR_CUDA;
+    }
+    if (slot < 0) {
+        slot = (g_used < kMaxContexts) ? g_used++ : (int)(((uintptr_t)ctx >> 4) % kMaxContexts);
+        g_addr[slot].ctx = ctx;
+    }
+    g_addr[slot].addr = p;
+    *out = p;
     return HZ_OK;
 }
 
@@ -87,14 +131,14 @@ extern "C" int hz_matvec_f64_noalloc(const hz_params *p, int64_t n, int adjoint,
         set_error("hz_matvec_f64_noalloc: NULL pointer");
         return HZ_ERR_ARG;
     }
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
     void *base = nullptr;
-    HZ_TRY(scratch_address(&base));
+    HZ_TRY(scratch_address(s, &base));
     unsigned char *b = static_cast<unsigned char *>(base);
     double4_32a *pos = reinterpret_cast<double4_32a *>(b);
     double4_32a *nr = reinterpret_cast<double4_32a *>(b + kRecBytes);
     double2 *dens = reinterpret_cast<double2 *>(b + 2 * kRecBytes);
     unsigned *err = reinterpret_cast<unsigned *>(b + 3 * kRecBytes);
-    cudaStream_t s = static_cast<cudaStream_t>(stream);
     // the array keeps the previous call's contents: records and densities
     // are rewritten for c < n below, the error word must start at zero
     HZ_CHECK_CUDA(cudaMemsetAsync(err, 0, sizeof(unsigned), s));

@@ -55,9 +55,11 @@ int dense_bicg_ragged(int size, double *density, double *densityimg, double **K,
         memcpy(aim.data() + i * n, Ki[i], n * sizeof(double));
     }
     hz_solve_info info;
-    // BICGSTAB.h:12 DEFAULTACC
-    return hz_dense_bicg((int64_t)n, are.data(), aim.data(), b, bimg, density, densityimg, 1e-7, maxit, HZ_HOST,
-                         &info);
+    // BICGSTAB.h:12 DEFAULTACC (hz_ref_config.bicg_acc)
+    hz_ref_config c;
+    hz_ref_get_config(&c);
+    return hz_dense_bicg((int64_t)n, are.data(), aim.data(), b, bimg, density, densityimg, c.bicg_acc, maxit,
+                         HZ_HOST, &info);
 }
 
 }  // namespace
@@ -136,7 +138,7 @@ __attribute__((weak, visibility("default"))) double WAVE = 15.0;
 namespace {
 
 // frame.h / PDE.h values of the reference build
-hz_ref_config g_ref = {-2.0, 2.0, 2.0, 0, 0, 1, 0, 0, 0, 1.0, {0.0, 0.0, 0.0}};
+hz_ref_config g_ref = {-2.0, 2.0, 2.0, 0, 0, 1, 0, 0, 0, 1.0, {0.0, 0.0, 0.0}, 1e-7};
 
 struct DeviceGrids {
     hz::DevBuf buf;

@@ -2,8 +2,9 @@
 // after P. T. P. Tang, "Table-lookup algorithms for elementary functions and
 // their error analysis" (1991): x = m (2 pi / 128) + r with |r| <= pi / 128,
 // sin/cos(m 2 pi / 128) from a 128-entry table in shared memory, sin/cos(r)
-// from their Taylor series (terms to r^7 and r^6; the first dropped terms
-// are below 1e-20), recombined by the angle-addition formulas.  Far shorter
+// from their Taylor series (terms to r^7 and r^6; the first dropped terms,
+// r^9/9! and r^8/8!, are below 1e-20 and 3.3e-18 at |r| = pi/128, about
+// 0.03 ulp of 1), recombined by the angle-addition formulas.  Far shorter
 // on GB300's FP64 pipe than a general sin/cos with its range reduction.
 #pragma once
 

@@ -5,6 +5,11 @@
 // (weno.c:259-345, distance_application3D.c:35-140,
 // finite_difference3D.c:220-721) on the same distance grid.
 //
+// The per-node helpers are __host__ __device__: the same code gives the
+// reference's per-node entry points on the host (weno, WENO_DX/DY/DZ,
+// BothCurvs, MeanCurv, GaussianCurv at the end of this file, built with
+// -ffp-contract=off so the host arithmetic is unfused as well).
+//
 // On GB300 these kernels are bound by the FP64 pipe (about 1.2 TFLOP/s,
 // roughly 1/60 of FP32), not by HBM: a node costs ~750 FP64 operations
 // (WENO weights need six IEEE divisions per axis, the cross derivatives
@@ -12,18 +17,19 @@
 // thread per node with read-only cached loads is therefore enough; the
 // neighbourhood is served by L1/L2.
 #include "hz_internal.cuh"
+#include "../../include/helmholtz_ref_api.h"
 
 namespace hz {
 namespace {
 
-__device__ __forceinline__ int mirror(int x, int N) { return x < 0 ? -x : (x > N ? 2 * N - x : x); }
+__host__ __device__ __forceinline__ int mirror(int x, int N) { return x < 0 ? -x : (x > N ? 2 * N - x : x); }
 
 // tools.c:296-310: max/min with the reference's tie and signed-zero rules.
-__device__ __forceinline__ double rmax(double a, double b) { return (a >= b) ? a : b; }
-__device__ __forceinline__ double rmin(double a, double b) { return (a <= b) ? a : b; }
+__host__ __device__ __forceinline__ double rmax(double a, double b) { return (a >= b) ? a : b; }
+__host__ __device__ __forceinline__ double rmin(double a, double b) { return (a <= b) ? a : b; }
 
 // weno.c:259-345
-__device__ void weno(double *dfp, double *dfn, const double *fi, double dx, int order)
+__host__ __device__ void weno(double *dfp, double *dfn, const double *fi, double dx, int order)
 {
     double aa, bb, cc, dd, ee, ff, df, ih;
     double IS0, IS1, IS2, a0, a1, a2, w0, w1, w2;
@@ -98,12 +104,12 @@ template <class A>
 struct Line {
     A a;
     long long base, stride;
-    __device__ double operator()(int m) const { return a(base + (long long)m * stride); }
+    __host__ __device__ double operator()(int m) const { return a(base + (long long)m * stride); }
 };
 
 // finite_difference3D.c:220-390; xorder selects XDER2's min_abs argument order.
 template <class L_>
-__device__ double der2(const L_ &L, int c, int N, double H, bool xorder)
+__host__ __device__ double der2(const L_ &L, int c, int N, double H, bool xorder)
 {
     double DDp, DDc, DDn;
     if (c == 0) return 2.0 * (L(1) - L(0)) / (H * H);
@@ -138,12 +144,12 @@ template <class A>
 struct Plane {
     A a;
     long long base, sa, sb;
-    __device__ double operator()(int u, int v) const { return a(base + (long long)u * sa + (long long)v * sb); }
+    __host__ __device__ double operator()(int u, int v) const { return a(base + (long long)u * sa + (long long)v * sb); }
 };
 
 // finite_difference3D.c:393-721 (secondpartialxy/xz/yz).
 template <class P_>
-__device__ double cross(const P_ &P, int ca, int cb, int N, double H)
+__host__ __device__ double cross(const P_ &P, int ca, int cb, int N, double H)
 {
     const double coef[3] = {1.0, -4.0, 3.0};
     if ((ca == 0) || (ca == N) || (cb == 0) || (cb == N)) return 0.0;
@@ -186,7 +192,7 @@ __device__ double cross(const P_ &P, int ca, int cb, int N, double H)
 // Gradient (gx, gy, gz) and curvatures (mc, gc) of one node (i, j, k),
 // o = its linear index, from the grid accessor acc.
 template <class A>
-__device__ __forceinline__ void grid_node(const A &acc, int N, double H, int i, int j, int k, long long o, int order,
+__host__ __device__ __forceinline__ void grid_node(const A &acc, int N, double H, int i, int j, int k, long long o, int order,
                                           bool want_grad, bool want_curv, double out[5])
 {
     const long long S = N + 1;
@@ -410,3 +416,86 @@ int launch_grid_stencils(int N, double H, const double *d, double *gx, double *g
 }
 
 }  // namespace hz
+
+// ---- The reference's per-node entry points, on the host ------------------
+// weno.h:26-31 and distance_application3D.h:9-11, with the reference's C++
+// signatures (so their mangled names equal the reference objects').  A GPU
+// cannot speed up a call that computes one node; these keep the reference's
+// per-node API for drivers that loop over nodes themselves, with the same
+// arithmetic as the whole-grid kernels above.
+namespace {
+// The reference's ragged grid uvalue[i][j][k], i, j, k in [0, N].
+struct RaggedAcc {
+    double ***d;
+    long long S;
+    double operator()(long long q) const { return d[q / (S * S)][(q / S) % S][q % S]; }
+};
+
+void weno_line(double ***u, int i, int j, int k, int N, double H, double *up, double *un, int order, int axis)
+{
+    // weno.c:117-254: only orders 5 and 3 are handled; other orders leave
+    // the outputs as they are
+    if (order != 5 && order != 3) return;
+    const int half = (order == 5) ? 3 : 2;
+    double f[7];
+    for (int m = -half; m <= half; m++) {
+        if (axis == 0) f[m + half] = u[i][hz::mirror(j + m, N)][k];
+        else if (axis == 1) f[m + half] = u[hz::mirror(i + m, N)][j][k];
+        else f[m + half] = u[i][j][hz::mirror(k + m, N)];
+    }
+    hz::weno(up, un, f, H, order);
+}
+}  // namespace
+
+// weno.c:259-345
+void weno(double *dfp, double *dfn, double fi[], const double dx, const int order)
+{
+    hz::weno(dfp, dfn, fi, dx, order);
+}
+
+// weno.c:117-254: one-sided WENO derivatives along x (index j), y (i), z (k),
+// mirror images across the grid's faces.
+void WENO_DX(double ***uvalue, const int i, const int j, const int k, const int N, const double H, double *ux_p,
+             double *ux_n, const int order)
+{
+    weno_line(uvalue, i, j, k, N, H, ux_p, ux_n, order, 0);
+}
+
+void WENO_DY(double ***uvalue, const int i, const int j, const int k, const int N, const double H, double *ux_p,
+             double *ux_n, const int order)
+{
+    weno_line(uvalue, i, j, k, N, H, ux_p, ux_n, order, 1);
+}
+
+void WENO_DZ(double ***uvalue, const int i, const int j, const int k, const int N, const double H, double *ux_p,
+             double *ux_n, const int order)
+{
+    weno_line(uvalue, i, j, k, N, H, ux_p, ux_n, order, 2);
+}
+
+// distance_application3D.c:35-53
+int BothCurvs(double ***dist, int i, int j, int k, int N, double H, double *meancurv, double *gausscurv)
+{
+    const long long S = N + 1;
+    double out[5];
+    hz::grid_node(RaggedAcc{dist, S}, N, H, i, j, k, ((long long)i * S + j) * S + k, 5, false, true, out);
+    *meancurv = out[3];
+    *gausscurv = out[4];
+    return 0;
+}
+
+// distance_application3D.c:4-21
+double GaussianCurv(double ***dist, int i, int j, int k, int N, double H)
+{
+    double m = 0.0, g = 0.0;
+    BothCurvs(dist, i, j, k, N, H, &m, &g);
+    return g;
+}
+
+// distance_application3D.c:23-33
+double MeanCurv(double ***dist, int i, int j, int k, int N, double H)
+{
+    double m = 0.0, g = 0.0;
+    BothCurvs(dist, i, j, k, N, H, &m, &g);
+    return m;
+}

@@ -271,11 +271,12 @@ __global__ void __launch_bounds__(NT, MINB) sweep32_kernel(Args32 a)
             for (int g = 0; g < TG; g++)
                 rel[g] = make_float3((th[g].x - oh.x) + (tl[g].x - ol.x), (th[g].y - oh.y) + (tl[g].y - ol.y),
                                      (th[g].z - oh.z) + (tl[g].z - ol.z));
-            const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((it >> 1) & 1), kWaitLimit);
+            const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((it >> 1) & 1), g_data_wait_limit);
             if (__syncthreads_or(!ok)) {
                 if (threadIdx.x == 0) {
                     atomicOr(a.err, DEV_ERR_WAIT);
-                    if (u + 1 < u_end) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimit);
+                    mbar_drain(&bar[buf], (uint32_t)((it >> 1) & 1), &bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1),
+                               u + 1 < u_end);
                 }
                 return;
             }
@@ -442,11 +443,12 @@ __device__ __forceinline__ bool batch_tiles(const Args32 &a, const BatchOp *ops,
         for (int g = 0; g < TG; g++)
             rel[g] = make_float3((th[g].x - oh.x) + (tl[g].x - ol.x), (th[g].y - oh.y) + (tl[g].y - ol.y),
                                  (th[g].z - oh.z) + (tl[g].z - ol.z));
-        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((it >> 1) & 1), kWaitLimit);
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((it >> 1) & 1), g_data_wait_limit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
                 atomicOr(a.err, DEV_ERR_WAIT);
-                if (u + 1 < u_end) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1), kWaitLimit);
+                mbar_drain(&bar[buf], (uint32_t)((it >> 1) & 1), &bar[buf ^ 1], (uint32_t)(((it + 1) >> 1) & 1),
+                           u + 1 < u_end);
             }
             return false;
         }
@@ -891,5 +893,7 @@ int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int
     if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
     return HZ_OK;
 }
+
+HZ_DEFINE_WAIT_LIMIT_SETTER(set_wait_limit_f32)
 
 }  // namespace hz

@@ -99,12 +99,13 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
     for (int64_t tile = 0; tile < ntiles; tile++) {
         const int buf = (int)(tile & 1);
         if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
-        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), g_data_wait_limit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
                 atomicOr(a.err, DEV_ERR_WAIT);
-                // let an issued copy land before the block exits (bounded)
-                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
+                // let the issued copies land before the block exits (bounded)
+                mbar_drain(&bar[buf], (uint32_t)((tile >> 1) & 1), &bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1),
+                           tile + 1 < ntiles);
             }
             return;
         }
@@ -225,5 +226,7 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
     return HZ_OK;
 }
+
+HZ_DEFINE_WAIT_LIMIT_SETTER(set_wait_limit_f64)
 
 }  // namespace hz

@@ -167,11 +167,12 @@ __global__ void __launch_bounds__(kNT32m, RB <= 8 ? 2 : 1) sweepm32_kernel(ArgsM
         const float4 oh = a.ohi[tile], ol = a.olo[tile];
         const float3 rel = make_float3((th.x - oh.x) + (tl.x - ol.x), (th.y - oh.y) + (tl.y - ol.y),
                                        (th.z - oh.z) + (tl.z - ol.z));
-        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), g_data_wait_limit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
                 atomicOr(a.err, DEV_ERR_WAIT);
-                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
+                mbar_drain(&bar[buf], (uint32_t)((tile >> 1) & 1), &bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1),
+                           tile + 1 < ntiles);
             }
             return;
         }
@@ -285,11 +286,12 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
     for (int64_t tile = 0; tile < ntiles; tile++) {
         const int buf = (int)(tile & 1);
         if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
-        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), kWaitLimit);
+        const bool ok = mbar_wait_bounded(&bar[buf], (uint32_t)((tile >> 1) & 1), g_data_wait_limit);
         if (__syncthreads_or(!ok)) {
             if (threadIdx.x == 0) {
                 atomicOr(a.err, DEV_ERR_WAIT);
-                if (tile + 1 < ntiles) mbar_wait_bounded(&bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1), kWaitLimit);
+                mbar_drain(&bar[buf], (uint32_t)((tile >> 1) & 1), &bar[buf ^ 1], (uint32_t)(((tile + 1) >> 1) & 1),
+                           tile + 1 < ntiles);
             }
             return;
         }
@@ -476,5 +478,7 @@ int sweep_multi(const SweepConst &c, const Rec32 &r32, const Rec64 &r64, int pre
     }
     return HZ_OK;
 }
+
+HZ_DEFINE_WAIT_LIMIT_SETTER(set_wait_limit_multi)
 
 }  // namespace hz

@@ -53,7 +53,8 @@ extern "C" {
 
 /* Arithmetic of a matvec or solve. */
 #define HZ_PREC_F64 0         /* plain FP64 everywhere                                  */
-#define HZ_PREC_F32 1         /* FP32 pair sweep (tile-local origins, split phase),
+#define HZ_PREC_F32 1         /* FP32 pair sweep (tile-local origins; phase k rho passed
+                                 to the SFU sin/cos, or split-k with hz_set_phase_mode),
                                  FP64 inner products                                    */
 #define HZ_PREC_F32_REFINED 2 /* FP32 inner solves inside FP64 iterative refinement whose
                                  residual b - A x uses the FP64 sweep                   */
@@ -101,8 +102,12 @@ typedef struct hz_solve_opts {
     int maxit;         /* Krylov iteration cap (reference: 2000)                        */
     double inner_tol;  /* HZ_PREC_F32_REFINED: relative tolerance of each inner solve
                           (FP32 densities bound it near 1e-7; an inner solve also
-                          stops after 30 iterations without a new minimum)       */
-    int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap                      */
+                          stops once it has run max(30, iterations to its last new
+                          minimum) iterations without a new minimum, and returns
+                          its best iterate)                                             */
+    int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap; refinement also
+                          stops, keeping its best iterate, when a step does not
+                          lower the FP64 residual                                      */
     int stagnation;    /* 1: also stop when |delta(||r||/||b||)| < 1e-3 tol (reference) */
     int restart;       /* HZ_GMRES: Krylov basis size before a restart (2..127)         */
 } hz_solve_opts;
@@ -115,6 +120,13 @@ typedef struct hz_solve_info {
     double seconds;       /* wall time of the solve                               */
     int64_t pair_evals;   /* kernel pair evaluations performed                    */
     int status;           /* HZ_OK, or why it stopped early                       */
+    int converged;        /* 1 when the final residual (resid_f64 for refined
+                             solves) is below tol, 0 when the solve stopped at
+                             its iteration or refinement cap, on stagnation, or
+                             (refined) when a refinement step stopped reducing
+                             the FP64 residual; the call still returns HZ_OK and
+                             its best iterate, as the reference's CompBiCG
+                             returns after its last iteration                     */
 } hz_solve_info;
 
 HZ_API const char *hz_last_error(void);
@@ -381,6 +393,15 @@ HZ_API int hz_set_combo(hz_operator *op, const hz_dense_opts *o);
  * launches count their kernels), for launch accounting. */
 HZ_API int64_t hz_kernel_launches(void);
 
+/* Poll limit of the pair sweeps' data waits (a CTA waiting for the bulk
+ * copy of its next source tile) on the current device; polls < 0 restores
+ * the default (2^24 polls, far above any real wait).  A wait that runs out
+ * sets the device error word, the CTA lets its copies in flight land
+ * (those waits keep the full bound) and exits, and the call returns
+ * HZ_ERR_DEVICE_WAIT with the context still usable.  A short limit (0 gives
+ * up at once) exercises that error path in tests. */
+HZ_API int hz_set_wait_limit(long long polls);
+
 /* Allocation-free FP64 product, for callers that cannot allocate device
  * memory when they need it (applications that hand out all device memory
  * from their own pools, plugin hosts that forbid allocation after start-up,
@@ -392,9 +413,11 @@ HZ_API int64_t hz_kernel_launches(void);
  * returns them.  It calls no cudaMalloc, cudaFree or allocating library
  * routine: its scratch is one fixed __device__ array of about 3 MiB that
  * every GPU loading this library holds until the process exits; n above
- * HZ_NOALLOC_MAX_POINTS is rejected with HZ_ERR_ARG.  The first call on a
- * device looks up that array's address with that device current, so make
- * the first call before any stream capture.  All calls share the array:
+ * HZ_NOALLOC_MAX_POINTS is rejected with HZ_ERR_ARG.  The array's device
+ * address belongs to the current CUDA context; each call looks it up again
+ * in the context current at the call (a host-side lookup, no allocation),
+ * so a context switch or cudaDeviceReset between calls is safe; the first
+ * call in a context must come before any stream capture.  All calls share the array:
  * calls that overlap on the GPU (other streams, other threads) race.  Work
  * is ordered on `stream` (NULL: the legacy default stream) and the call
  * waits for it to finish before returning its status. */

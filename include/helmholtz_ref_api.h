@@ -28,8 +28,38 @@ HZ_API int ASSIGN_GRADIENT(int N, double H, double ***dist, double ***graddx, do
  * reference calls BothCurvs once per node. */
 HZ_API int ASSIGN_CURVATURES(int N, double H, double ***dist, double ***mcurv, double ***gcurv);
 
+/* ---- Per-node functions, on the host -------------------------------------
+ * The reference's per-node entry points, for drivers that loop over nodes
+ * themselves (large3Dexample2.c:446-455 calls BothCurvs once per node).  A
+ * GPU cannot speed up one node per call, so these run on the host in FP64
+ * with the arithmetic of the whole-grid kernels (unfused, in the
+ * reference's operation order: results bit-identical to the reference's).
+ * Grids are the reference's ragged [N+1][N+1][N+1] arrays. */
+
+/* weno.h:31, weno.c:259-345: WENO3 (order 3, fi[0..4]) or WENO5 (any other
+ * order, fi[0..6]) one-sided derivatives at the centre of fi, spacing dx. */
+HZ_API void weno(double *dfp, double *dfn, double fi[], const double dx, const int order);
+
+/* weno.h:26-28, weno.c:117-254: WENO one-sided derivatives of uvalue at node
+ * (i, j, k) along x (index j), y (index i), z (index k), mirrored across the
+ * grid's faces; order 5 or 3 (other orders leave the outputs unchanged). */
+HZ_API void WENO_DX(double ***uvalue, const int i, const int j, const int k, const int N, const double H,
+                    double *ux_p, double *ux_n, const int order);
+HZ_API void WENO_DY(double ***uvalue, const int i, const int j, const int k, const int N, const double H,
+                    double *ux_p, double *ux_n, const int order);
+HZ_API void WENO_DZ(double ***uvalue, const int i, const int j, const int k, const int N, const double H,
+                    double *ux_p, double *ux_n, const int order);
+
+/* distance_application3D.h:9-11, distance_application3D.c:4-53: Gaussian and
+ * mean curvature of the distance grid at node (i, j, k) from the limited
+ * second differences (finite_difference3D.c:220-721); BothCurvs returns 0. */
+HZ_API double GaussianCurv(double ***dist, int i, int j, int k, int N, double H);
+HZ_API double MeanCurv(double ***dist, int i, int j, int k, int N, double H);
+HZ_API int BothCurvs(double ***dist, int i, int j, int k, int N, double H, double *meancurv, double *gausscurv);
+
 /* BICGSTAB.h:15 -- complex BiCG on a dense caller-owned matrix
- * (BICGSTAB.c:5-339): tolerance DEFAULTACC = 1e-7, at most 1000 iterations. */
+ * (BICGSTAB.c:5-339): tolerance DEFAULTACC (hz_ref_config.bicg_acc, 1e-7),
+ * at most 1000 iterations. */
 HZ_API int CompBiCG(int size, double *density, double *densityimg, double **Kernel, double **Kernelimg,
                     double *b, double *bimg);
 
@@ -91,6 +121,8 @@ typedef struct hz_ref_config {
     int combo_interior;      /* PDE.h COMBO_INTERIOR                (0) */
     double radius;           /* frame.h radius                      (1) */
     double center[3];        /* frame.h Cx, Cy, Cz            (0, 0, 0) */
+    double bicg_acc;         /* BICGSTAB.h DEFAULTACC: CompBiCG and
+                                omp_CompBiCG stop at ||r||/||b|| below it (1e-7) */
 } hz_ref_config;
 
 #ifdef __cplusplus
