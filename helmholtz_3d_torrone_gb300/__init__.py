@@ -84,16 +84,26 @@ class RefConfig(C.Structure):
                 ("bicg_acc", C.c_double)]
 
 
+MAX_STEPS = 8  # HZ_MAX_STEPS
+
+
 class SolveInfo(C.Structure):
     """hz_solve_info: iterations (inner ones for refined solves), refinement
     steps, final relative residual (FP64 for refined solves), seconds, pair
-    evaluations, status and whether the final residual is below tol."""
+    evaluations, status, whether the final residual is below tol, and per
+    refinement step its inner iterations, inner tolerance and FP64 residual."""
     _fields_ = [("iterations", C.c_int), ("outer", C.c_int), ("resid", C.c_double), ("resid_f64", C.c_double),
-                ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int), ("converged", C.c_int)]
+                ("seconds", C.c_double), ("pair_evals", C.c_int64), ("status", C.c_int), ("converged", C.c_int),
+                ("steps", C.c_int), ("step_iters", C.c_int * MAX_STEPS),
+                ("step_inner_tol", C.c_double * MAX_STEPS), ("step_resid", C.c_double * MAX_STEPS)]
 
     def as_dict(self):
-        """The fields as a dict."""
-        return {f: getattr(self, f) for f, _ in self._fields_}
+        """The fields as a dict (the per-step arrays cut to the steps taken)."""
+        out = {}
+        for f, _ in self._fields_:
+            v = getattr(self, f)
+            out[f] = list(v)[:self.steps] if f.startswith("step_") else v
+        return out
 
 
 _lib = None

@@ -367,6 +367,7 @@ int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts_in, const double *cons
     HZ_TRY(gather(b, b_im, B1, where, s));
     HZ_TRY(b->multi.reserve(nm, R));
     std::vector<double> res(R, 0.0);
+    hz_solve_info inf{};
     int iters = 0, outer = 0;
     long long pairs = 0;
     std::vector<int> cit;
@@ -421,8 +422,9 @@ int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts_in, const double *cons
             }
             int it = 0;
             std::vector<double> ires;
-            HZ_TRY(b->multi.solve(A32, Q0, Q1, o.inner_tol, o.maxit, o.stagnation != 0, s, it, ires,
-                                  kInnerStallBatch, &cit));
+            const double itol = refine_inner_tol(o, worst());
+            HZ_TRY(b->multi.solve(A32, Q0, Q1, itol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStallBatch,
+                                  &cit));
             iters += it;
             pairs += pairs_of(cit, 2);
             A64.cols = open;
@@ -439,13 +441,18 @@ int hz_batch_solve(hz_batch *b, const hz_solve_opts *opts_in, const double *cons
                 HZ_TRY(vec_norm(nm, R0 + off, R1 + off, part, dout, nr[r], s));
                 res[r] = normb[r] > 0 ? nr[r] / normb[r] : 0.0;
             }
+            if (inf.steps < HZ_MAX_STEPS) {
+                inf.step_iters[inf.steps] = it;
+                inf.step_inner_tol[inf.steps] = itol;
+                inf.step_resid[inf.steps] = worst();
+                inf.steps++;
+            }
         }
     }
     HZ_TRY(scatter(b, X0, x_re, where, s));
     HZ_TRY(scatter(b, X1, x_im, where, s));
     HZ_CHECK_CUDA(cudaStreamSynchronize(s));
     const int rc = batch_errors(b, "hz_batch_solve");
-    hz_solve_info inf{};
     double w = 0;
     for (int r = 0; r < R; r++) {
         w = res[r] > w ? res[r] : w;

@@ -953,7 +953,8 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
             }
             int it = 0;
             std::vector<double> ires;
-            HZ_TRY(st->multi.solve(A32, Q0, Q1, o.inner_tol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStall));
+            const double itol = refine_inner_tol(o, worst());
+            HZ_TRY(st->multi.solve(A32, Q0, Q1, itol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStall));
             iters += it;
             for (int r : open)
                 HZ_TRY(vec_axpy(n, nr[r], st->multi.re(KrylovMulti::X) + r * n, st->multi.im(KrylovMulti::X) + r * n,
@@ -964,6 +965,12 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
                 HZ_TRY(vec_sub(n, B0 + r * n, B1 + r * n, Q0 + r * n, Q1 + r * n, R0 + r * n, R1 + r * n, s));
                 HZ_TRY(vec_norm(n, R0 + r * n, R1 + r * n, part, dout, nr[r], s));
                 res[r] = normb[r] > 0 ? nr[r] / normb[r] : 0.0;
+            }
+            if (inf.steps < HZ_MAX_STEPS) {
+                inf.step_iters[inf.steps] = it;
+                inf.step_inner_tol[inf.steps] = itol;
+                inf.step_resid[inf.steps] = worst();
+                inf.steps++;
             }
         }
         pairs = A32.pairs + A64.pairs;
@@ -1111,18 +1118,19 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         HZ_TRY(vec_scale(n, 1.0 / nr, r0, r1, q0, q1, s));
         int it = 0, ist = HZ_OK;
         double ires = 0.0;
+        const double itol = refine_inner_tol(o, res);
         const double *e0, *e1;
         if (gm) {
             int prods = 0;
             double *g0 = st->gx.as<double>(), *g1 = g0 + n;
-            HZ_TRY(gmres_solve(A32, n, o.restart, q0, q1, g0, g1, o.inner_tol, o.maxit, kInnerStall, st->gwork,
-                               st->gsmall, s, it, ires, prods));
+            HZ_TRY(gmres_solve(A32, n, o.restart, q0, q1, g0, g1, itol, o.maxit, kInnerStall, st->gwork, st->gsmall,
+                               s, it, ires, prods));
             products += prods;
             e0 = g0;
             e1 = g1;
         } else {
-            HZ_TRY(st->inner.solve(A32, o.method, q0, q1, o.inner_tol, o.maxit, o.stagnation != 0, true, s, it, ires,
-                                   ist, kInnerStall));
+            HZ_TRY(st->inner.solve(A32, o.method, q0, q1, itol, o.maxit, o.stagnation != 0, true, s, it, ires, ist,
+                                   kInnerStall));
             products += 2LL * it;
             e0 = st->inner.re(Krylov::X);
             e1 = st->inner.im(Krylov::X);
@@ -1139,6 +1147,12 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         HZ_TRY(vec_norm(n, r0, r1, part, dout, nr, s));
         A64.iteration_done(false);
         res = nr / normb;
+        if (inf.steps < HZ_MAX_STEPS) {
+            inf.step_iters[inf.steps] = it;
+            inf.step_inner_tol[inf.steps] = itol;
+            inf.step_resid[inf.steps] = res;
+            inf.steps++;
+        }
         if (!(res < best)) {
             // no progress (or a non-finite residual): back to the best iterate
             if (outer > 1) {

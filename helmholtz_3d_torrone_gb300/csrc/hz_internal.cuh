@@ -288,4 +288,16 @@ namespace hz {
 int check_device_error(hz_operator *op, const char *where);
 hz::SweepConst sweep_const(const hz_operator *op);
 hz::Rec64 rec64(hz_operator *op);
+
+// Inner tolerance of a refinement step that starts from the FP64 relative
+// residual res: the factor by which the residual still has to fall, with a
+// margin of 4, clamped to [opts.inner_tol, 0.5].  The first step (res = 1)
+// solves to max(inner_tol, tol / 4); a step that only has to close a small
+// gap stops after a few iterations instead of repeating a full solve.
+inline double refine_inner_tol(const hz_solve_opts &o, double res)
+{
+    double t = (res > 0) ? o.tol / (4.0 * res) : 0.5;
+    if (t > 0.5) t = 0.5;
+    return t > o.inner_tol ? t : o.inner_tol;
+}
 }  // namespace hz

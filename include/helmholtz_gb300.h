@@ -100,17 +100,21 @@ typedef struct hz_solve_opts {
     int precision;     /* HZ_PREC_*                                                     */
     double tol;        /* stop at ||b - A x|| / ||b|| < tol (reference DEFAULTACC 1e-7) */
     int maxit;         /* Krylov iteration cap (reference: 2000)                        */
-    double inner_tol;  /* HZ_PREC_F32_REFINED: relative tolerance of each inner solve
-                          (FP32 densities bound it near 1e-7; an inner solve also
-                          stops once it has run max(30, iterations to its last new
-                          minimum) iterations without a new minimum, and returns
-                          its best iterate)                                             */
+    double inner_tol;  /* HZ_PREC_F32_REFINED: the tightest relative tolerance of an
+                          inner solve (FP32 densities bound it near 1e-7).  Step k
+                          solves to max(inner_tol, min(0.5, tol / (4 res_{k-1}))),
+                          res_0 = 1: only as far as the FP64 residual still has
+                          to fall.  An inner solve also stops once it has run
+                          max(30, iterations to its last new minimum) iterations
+                          without a new minimum, and returns its best iterate    */
     int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap; refinement also
                           stops, keeping its best iterate, when a step does not
                           lower the FP64 residual                                      */
     int stagnation;    /* 1: also stop when |delta(||r||/||b||)| < 1e-3 tol (reference) */
     int restart;       /* HZ_GMRES: Krylov basis size before a restart (2..127)         */
 } hz_solve_opts;
+
+#define HZ_MAX_STEPS 8
 
 typedef struct hz_solve_info {
     int iterations;       /* Krylov iterations in total (inner ones when refined) */
@@ -127,6 +131,11 @@ typedef struct hz_solve_info {
                              the FP64 residual; the call still returns HZ_OK and
                              its best iterate, as the reference's CompBiCG
                              returns after its last iteration                     */
+    /* refined solves: the first HZ_MAX_STEPS refinement steps, one entry each */
+    int steps;                           /* entries filled (min(outer, HZ_MAX_STEPS)) */
+    int step_iters[HZ_MAX_STEPS];        /* inner Krylov iterations of the step       */
+    double step_inner_tol[HZ_MAX_STEPS]; /* inner tolerance the step solved to        */
+    double step_resid[HZ_MAX_STEPS];     /* FP64 relative residual after the step     */
 } hz_solve_info;
 
 HZ_API const char *hz_last_error(void);

@@ -24,10 +24,13 @@ Variants:
   dirichlet : [-1,1]^3, FACTOR 3, TAU_FACTOR 2, Dirichlet, exterior;
               BiCG tolerance 1e-13.
 
-Usage: python oracle/build_ref.py [--ref /root/reference] [--stage-only]
-The staged sources stay in oracle/_ref/src so that a machine without the
+Usage: python oracle/build_ref.py [--ref DIR] [--stage-only | --from-stage | --auto]
+DIR is the reference tree: --ref, else the HZ_REFERENCE_DIR environment
+variable, else DEFAULT_REF below (where this container mounts it).  The
+staged sources stay in oracle/_ref/src so that a machine without the
 reference tree (the GPU host) can still compile the variants
-(python oracle/build_ref.py --from-stage).
+(python oracle/build_ref.py --from-stage).  --auto builds from the tree when
+it exists, else from the staged sources, else does nothing.
 """
 import argparse
 import os
@@ -38,6 +41,7 @@ import sys
 from concurrent.futures import ThreadPoolExecutor
 
 HERE = os.path.dirname(os.path.abspath(__file__))
+DEFAULT_REF = "/root/reference"
 OUT = os.path.join(HERE, "_ref")
 SRC = os.path.join(OUT, "src")
 
@@ -124,11 +128,22 @@ def compile_variant(name, jobs):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--ref", default=os.environ.get("HZ_REFERENCE_DIR", "/root/reference"))
-    ap.add_argument("--from-stage", action="store_true")
-    ap.add_argument("--stage-only", action="store_true")
+    ap.add_argument("--ref", default=os.environ.get("HZ_REFERENCE_DIR", DEFAULT_REF),
+                    help="the reference tree (default: $HZ_REFERENCE_DIR, else %s)" % DEFAULT_REF)
+    ap.add_argument("--from-stage", action="store_true", help="compile the sources staged under oracle/_ref/src")
+    ap.add_argument("--stage-only", action="store_true", help="copy and patch the sources, do not compile")
+    ap.add_argument("--auto", action="store_true",
+                    help="the tree if it exists, else the staged sources, else nothing (exit 0)")
     ap.add_argument("-j", type=int, default=os.cpu_count() or 4)
     a = ap.parse_args()
+    if a.auto:
+        if os.path.isdir(a.ref):
+            a.from_stage = False
+        elif os.path.isdir(SRC):
+            a.from_stage = True
+        else:
+            print("no reference tree and no staged sources: reference build skipped", file=sys.stderr)
+            return 0
     if not a.from_stage:
         if not os.path.isdir(a.ref):
             print("reference tree %s not found" % a.ref, file=sys.stderr)

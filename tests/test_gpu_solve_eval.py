@@ -91,3 +91,37 @@ def test_config1_point_source_kat(hz, oracle, precision):
         xo, it, res = oracle.bicg(po, tp, bo, acc=1e-8)
         assert rel_err(x, xo) < 1e-6
     op.close()
+
+
+@pytest.mark.parametrize("precision", ["f64", "refined"])
+def test_config1_density_vs_reference_compbicg(hz, precision):
+    """Benchmark configuration 1 against the reference's own solve: the
+    reference build assembled its dense matrix (omp_get_Ccomp entries) for
+    the 64^3 sphere and ran CompBiCG (BICGSTAB.c:5-339) to 1e-13
+    (tests/golden/make_golden.py).  The GPU's FP64 BiCG to 1e-13, and its
+    FP32 + FP64-refinement solve to an FP64 residual of 1e-12, give the same
+    density to 1e-10 (max-norm relative)."""
+    import hashlib
+    import json
+    from conftest import golden
+    from helmholtz_3d_torrone_gb300 import geometry as G
+
+    g = golden("ref_dirichlet_sphere_n64_solve")
+    m = json.loads(str(g["meta"]))
+    d = G.sphere(m["N"], radius=m["radius"], center=tuple(m["center"]))
+    assert hashlib.sha256(d.tobytes()).hexdigest() == m["sha256"]["d"]
+    p = hz.params(m["N"], m["wave"], int_l=m["int_l"], int_u=m["int_u"], factor=m["factor"],
+                  tau_factor=m["tau_factor"], dirichlet=m["dirichlet"], interior=m["interior"])
+    with hz.Operator(p) as op:
+        op.set_distance(d)
+        assert op.build() == m["n"]
+        idx = op.tube()["idx"].astype(np.int64)
+        assert hashlib.sha256(idx.tobytes()).hexdigest() == m["sha256"]["idx"]
+        b = op.rhs_point_source(np.array(m["center"]), hz.RHS_POINT_DIRICHLET)
+        if precision == "f64":
+            x, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=1e-13, maxit=1000)
+            assert info["resid"] < 1e-13
+        else:
+            x, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F32_REFINED, tol=1e-12, inner_tol=1e-5)
+            assert info["resid_f64"] < 1e-12
+    assert rel_err(x, g["x"]) < 1e-10
