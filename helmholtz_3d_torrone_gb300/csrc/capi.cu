@@ -86,6 +86,7 @@ SweepConst sweep_const(const hz_operator *op)
     c.interior = op->p.interior;
     c.err = op->err.as<unsigned>();
     c.phase_split = op->phase_mode == HZ_PHASE_SPLIT;
+    c.extent = 1.7320508075688772 * (op->p.int_u - op->p.int_l);
     return c;
 }
 

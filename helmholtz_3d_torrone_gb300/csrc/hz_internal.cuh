@@ -120,6 +120,7 @@ struct SweepConst {
     int interior;
     unsigned *err;  // device error word
     int phase_split = 0;  // FP32 sweep: phase reduced with a split k/(2 pi) (HZ_PHASE_SPLIT)
+    double extent = 0.0;  // largest point distance: the domain's diagonal sqrt(3) (int_u - int_l)
 };
 
 // sweep modes

@@ -155,6 +155,7 @@ extern "C" int hz_matvec_f64_noalloc(const hz_params *p, int64_t n, int adjoint,
     c.dirichlet = p->dirichlet;
     c.interior = p->interior;
     c.err = err;
+    c.extent = 1.7320508075688772 * (p->int_u - p->int_l);
     Rec64 r;
     r.pos = pos;
     r.nrm = nr;

@@ -10,20 +10,26 @@
 //   A_tt += 1/2.
 // A^H row t uses conj(A_st) = w_t conj(...) with the roles of t and s swapped.
 //
-// One thread owns one target; source tiles of kTile64 records (position+reg,
-// normal+weight, prescaled density) are staged in shared memory by TMA bulk
-// copies, double-buffered on mbarriers.  FP64 throughout; the 1/2 diagonal
-// and the weights are applied in the epilogue.
+// One thread owns two targets (kTgt64); source tiles of kSrc64 records
+// (position+reg, normal+weight, prescaled density) are staged in shared
+// memory by TMA bulk copies, double-buffered on mbarriers, and each staged
+// record serves both targets.  FP64 throughout; the 1/2 diagonal and the
+// weights are applied in the epilogue.
 //
-// GB300 runs FP64 at about 1/60 of its FP32 rate, so the FP64 arithmetic is
-// kept short: 1/rho comes from rsqrt(rho^2) and rho = rho^2 / rho, and
-// sin/cos use the table-driven method of sincos64.cuh.  The near-field
-// decision keeps the reference's test sqrt(rho^2) > tau exactly: it is
-// evaluated whenever rho^2 lies within a relative 1e-12 of tau^2, where
-// rho^2 > tau^2 could disagree.
+// GB300 runs FP64 at about 1/64 of its FP32 rate and the kernel is bound by
+// the FP64 pipe, so each far pair costs as few FP64 operations as the
+// result's accuracy allows (pair64.cuh): 1/rho from an SFU seed and one
+// third-order correction, sin/cos of k rho from a 2048-entry table and two
+// short series, the table index from FP32 arithmetic, and the entry formed
+// as e^{i k rho} (-1/rho + i k) / rho^2 (six FP64 multiplies fewer than the
+// reference's separate ct1 and ct2).  The near-field decision keeps the
+// reference's test sqrt(rho^2) > tau exactly: rho^2 and tau^2 are compared
+// as integers (their bit patterns order like the values), and within 8192
+// ulps of tau^2 the reference's own arithmetic (rho^2 summed without fused
+// multiply-adds, IEEE square root) decides.
 #include "hz_internal.cuh"
 #include "bulk_copy.cuh"
-#include "sincos64.cuh"
+#include "pair64.cuh"
 
 namespace hz {
 namespace {
@@ -31,6 +37,8 @@ namespace {
 struct Args64 {
     int64_t n;
     double wave, tau, tau2;
+    float kscale;       // k * 2048 / (2 pi): the phase table index in FP32
+    long long tau2b;    // bit pattern of tau^2
     double inv_scale;  // 4 pi sg: the near-field value times this cancels the density prescale
     const double4_32a *pos, *nrm;
     const double4_32a *dens;  // (w_s p_re, w_s p_im, pt_re, pt_im)
@@ -38,6 +46,10 @@ struct Args64 {
     double *q_re, *q_im, *qt_re, *qt_im;
     unsigned *err;
 };
+
+constexpr int kSrc64 = 64;   // sources per shared-memory tile
+constexpr int kTgt64 = 2;    // targets per thread
+constexpr long long kTieUlps = 8192;
 
 // dens = scale (w p, pt), scale = sg / (4 pi): the kernel's common factor.
 __global__ void prep64_kernel(int64_t n, const double4_32a *__restrict__ nrm, const double *__restrict__ p_re,
@@ -61,23 +73,73 @@ __global__ void prep64_kernel(int64_t n, const double4_32a *__restrict__ nrm, co
 
 constexpr double kPi64 = 3.14159265358979323846264338328;
 
+// One (target, source) pair added to acc = (A re, A im, A^H re, A^H im).
 template <int MODE, bool DIR>
-__global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
+__device__ __forceinline__ void pair64(const Args64 &a, const double2 *tab, const double4_32a &tp,
+                                       const double4_32a &tn, const double4_32a &sp, const double4_32a &sn,
+                                       const double4_32a &sd, double *acc)
 {
-    constexpr int T = kTile64;
+    const double dx = tp.x - sp.x, dy = tp.y - sp.y, dz = tp.z - sp.z;
+    const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
+    const long long rb = __double_as_longlong(r2);
+    bool far = rb > a.tau2b;
+    if ((unsigned long long)(rb - a.tau2b + kTieUlps) <= (unsigned long long)(2 * kTieUlps)) {
+        const double r2ref = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+        far = __dsqrt_rn(r2ref) > a.tau;
+    }
+    if (far) {
+        double ur, ui, y2;
+        far_factor64(r2, a.wave, a.kscale, tab, ur, ui, y2);
+        if (MODE & SWEEP_A) {
+            const double in = DIR ? fma(dz, sn.z, fma(dy, sn.y, dx * sn.x)) : fma(dz, tn.z, fma(dy, tn.y, dx * tn.x));
+            const double f = in * y2;
+            const double vr = ur * f, vi = ui * f;
+            acc[0] = fma(-vi, sd.y, fma(vr, sd.x, acc[0]));
+            acc[1] = fma(vi, sd.x, fma(vr, sd.y, acc[1]));
+        }
+        if (MODE & SWEEP_AH) {
+            const double in = DIR ? fma(dz, tn.z, fma(dy, tn.y, dx * tn.x)) : fma(dz, sn.z, fma(dy, sn.y, dx * sn.x));
+            // conj of the entry with the roles swapped: in -> -in, imaginary part negated
+            const double f = -(in * y2);
+            const double vr = ur * f, vi = -(ui * f);
+            acc[2] = fma(-vi, sd.w, fma(vr, sd.z, acc[2]));
+            acc[3] = fma(vi, sd.z, fma(vr, sd.w, acc[3]));
+        }
+    } else {
+        if (MODE & SWEEP_A) {
+            const double v = (DIR ? sp.w : tp.w) * a.inv_scale;
+            acc[0] = fma(v, sd.x, acc[0]);
+            acc[1] = fma(v, sd.y, acc[1]);
+        }
+        if (MODE & SWEEP_AH) {
+            const double v = (DIR ? tp.w : sp.w) * a.inv_scale;
+            acc[2] = fma(v, sd.z, acc[2]);
+            acc[3] = fma(v, sd.w, acc[3]);
+        }
+    }
+}
+
+template <int MODE, bool DIR>
+__global__ void __launch_bounds__(kThreads64, 4) sweep64_kernel(Args64 a)
+{
+    constexpr int T = kSrc64;
     __shared__ alignas(128) double4_32a sp[2][T];
     __shared__ alignas(128) double4_32a sn[2][T];
     __shared__ alignas(128) double4_32a sd[2][T];
     __shared__ alignas(8) uint64_t bar[2];
-    __shared__ double2 tab[kSinTable];
-    fill_sin_table(tab);
-    const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    const bool valid = t < a.n;
-    double4_32a tp = make_double4_32a(0, 0, 0, 0), tn = make_double4_32a(0, 0, 0, 0);
-    if (valid) {
-        tp = a.pos[t];
-        tn = a.nrm[t];
+    __shared__ alignas(16) double2 tab[kPhaseTable];
+    fill_phase_table(tab);
+    const int64_t t0 = (int64_t)blockIdx.x * (blockDim.x * kTgt64) + threadIdx.x;
+    double4_32a tp[kTgt64], tn[kTgt64];
+    bool valid[kTgt64];
+#pragma unroll
+    for (int g = 0; g < kTgt64; g++) {
+        const int64_t t = t0 + (int64_t)g * blockDim.x;
+        valid[g] = t < a.n;
+        tp[g] = valid[g] ? a.pos[t] : make_double4_32a(0, 0, 0, 0);
+        tn[g] = valid[g] ? a.nrm[t] : make_double4_32a(0, 0, 0, 0);
     }
+    const bool any = valid[0];
     const int64_t ntiles = (a.n + T - 1) / T;
     if (threadIdx.x == 0) {
         mbar_init(&bar[0], 1);
@@ -95,7 +157,9 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
         bulk_g2s(&sd[buf][0], a.dens + base, bytes, &bar[buf]);
     };
     if (threadIdx.x == 0 && ntiles > 0) issue(0, 0);
-    double aAr = 0, aAi = 0, aHr = 0, aHi = 0;
+    double acc[kTgt64][4];
+#pragma unroll
+    for (int g = 0; g < kTgt64; g++) acc[g][0] = acc[g][1] = acc[g][2] = acc[g][3] = 0.0;
     for (int64_t tile = 0; tile < ntiles; tile++) {
         const int buf = (int)(tile & 1);
         if (threadIdx.x == 0 && tile + 1 < ntiles) issue(tile + 1, buf ^ 1);
@@ -111,76 +175,42 @@ __global__ void __launch_bounds__(kThreads64) sweep64_kernel(Args64 a)
         }
         const int64_t base = tile * T;
         const int cnt = (int)((a.n - base < T) ? (a.n - base) : T);
-        if (valid) {
+        if (any) {
             for (int j = 0; j < cnt; j++) {
                 const double4_32a sp_ = sp[buf][j];
                 const double4_32a sn_ = sn[buf][j];
                 const double4_32a sd_ = sd[buf][j];
-                const double xmy1 = tp.x - sp_.x, xmy2 = tp.y - sp_.y, xmy3 = tp.z - sp_.z;
-                const double r2 = xmy1 * xmy1 + xmy2 * xmy2 + xmy3 * xmy3;
-                bool far = r2 > a.tau2;
-                if (fabs(r2 - a.tau2) <= 1e-12 * a.tau2) far = sqrt(r2) > a.tau;
-                double vAr = 0.0, vAi = 0.0, vHr = 0.0, vHi = 0.0;
-                if (far) {
-                    const double rec = rsqrt(r2);
-                    const double rho = r2 * rec;
-                    double S, C;
-                    table_sincos(a.wave * rho, tab, S, C);
-                    // sg / (4 pi) rides on the densities
-                    const double eS = S * rec, eC = C * rec;
-                    const double denom = rec * rec;
-                    const double ct1 = -1. * (a.wave * S + eC) * denom;
-                    const double ct2 = (a.wave * C - eS) * denom;
-                    if (MODE & SWEEP_A) {
-                        const double in = DIR ? (xmy1 * sn_.x + xmy2 * sn_.y + xmy3 * sn_.z)
-                                              : (xmy1 * tn.x + xmy2 * tn.y + xmy3 * tn.z);
-                        vAr = ct1 * in;
-                        vAi = ct2 * in;
-                    }
-                    if (MODE & SWEEP_AH) {
-                        const double in = -(DIR ? (xmy1 * tn.x + xmy2 * tn.y + xmy3 * tn.z)
-                                                : (xmy1 * sn_.x + xmy2 * sn_.y + xmy3 * sn_.z));
-                        vHr = ct1 * in;
-                        vHi = -(ct2 * in);
-                    }
-                } else {
-                    vAr = (DIR ? sp_.w : tp.w) * a.inv_scale;
-                    vHr = (DIR ? tp.w : sp_.w) * a.inv_scale;
-                    vAi = 0.0;
-                    vHi = 0.0;
-                }
-                if (MODE & SWEEP_A) {
-                    aAr += vAr * sd_.x - vAi * sd_.y;
-                    aAi += vAr * sd_.y + vAi * sd_.x;
-                }
-                if (MODE & SWEEP_AH) {
-                    aHr += vHr * sd_.z - vHi * sd_.w;
-                    aHi += vHr * sd_.w + vHi * sd_.z;
-                }
+#pragma unroll
+                for (int g = 0; g < kTgt64; g++) pair64<MODE, DIR>(a, tab, tp[g], tn[g], sp_, sn_, sd_, acc[g]);
             }
         }
         __syncthreads();
     }
-    if (!valid) return;
-    if (MODE & SWEEP_A) {
-        double r = aAr, i = aAi;
-        if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
-        a.q_re[t] = r + 0.5 * a.p_re[t];
-        a.q_im[t] = i + 0.5 * a.p_im[t];
-    }
-    if (MODE & SWEEP_AH) {
-        const double w = tn.w;
-        double r = w * aHr, i = w * aHi;
-        if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
-        a.qt_re[t] = r + 0.5 * a.pt_re[t];
-        a.qt_im[t] = i + 0.5 * a.pt_im[t];
+#pragma unroll
+    for (int g = 0; g < kTgt64; g++) {
+        if (!valid[g]) continue;
+        const int64_t t = t0 + (int64_t)g * blockDim.x;
+        if (MODE & SWEEP_A) {
+            const double r = acc[g][0], i = acc[g][1];
+            if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
+            a.q_re[t] = r + 0.5 * a.p_re[t];
+            a.q_im[t] = i + 0.5 * a.p_im[t];
+        }
+        if (MODE & SWEEP_AH) {
+            const double w = tn[g].w;
+            const double r = w * acc[g][2], i = w * acc[g][3];
+            if (!isfinite(r) || !isfinite(i)) atomicOr(a.err, DEV_ERR_NONFINITE);
+            a.qt_re[t] = r + 0.5 * a.pt_re[t];
+            a.qt_im[t] = i + 0.5 * a.pt_im[t];
+        }
     }
 }
 
 template <int MODE>
 void launch64(const Args64 &a, bool dir, cudaStream_t s)
 {
-    const unsigned blocks = (unsigned)((a.n + kThreads64 - 1) / kThreads64);
+    const int per_block = kThreads64 * kTgt64;
+    const unsigned blocks = (unsigned)((a.n + per_block - 1) / per_block);
     if (dir) sweep64_kernel<MODE, true><<<blocks, kThreads64, 0, s>>>(a);
     else sweep64_kernel<MODE, false><<<blocks, kThreads64, 0, s>>>(a);
 }
@@ -193,6 +223,11 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
               cudaEvent_t ev1)
 {
     if (c.n <= 0) return HZ_OK;
+    if (!(c.wave * c.extent <= kMaxPhase64)) {
+        set_error("FP64 sweep: k * domain diagonal = %g exceeds the phase reduction's range (%g)",
+                  c.wave * c.extent, kMaxPhase64);
+        return HZ_ERR_ARG;
+    }
     double4_32a *dens = reinterpret_cast<double4_32a *>(scratch);
     const bool useA = (mode & SWEEP_A) != 0, useH = (mode & SWEEP_AH) != 0;
     {
@@ -211,6 +246,8 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     a.wave = c.wave;
     a.tau = c.tau;
     a.tau2 = c.tau * c.tau;
+    a.tau2b = (long long)__builtin_bit_cast(long long, a.tau2);
+    a.kscale = (float)(c.wave * (kPhaseTable / (2.0 * kPi64)));
     a.inv_scale = ((c.interior == 1) ? -1.0 : 1.0) * (4.0 * kPi64);
     a.pos = r.pos;
     a.nrm = r.nrm;

@@ -11,7 +11,9 @@ density for a point-source right-hand side solved to 1e-13.  The dense
 case holds the per-point arrays of the three dense assemblers of
 HelmholtzKernel.c, a sample of their matrix entries and their products with
 a seeded vector.  The Godunov case holds the reference's upwind |grad phi|
-(finite_difference3D.c:5-27) for seeded one-sided derivatives.
+(finite_difference3D.c:5-27) for seeded one-sided derivatives.  The digest
+case pins the reference's grid stages on the 256^3 torus by SHA-256 digests;
+the solve case holds the reference's CompBiCG density for the 64^3 sphere.
 
 Usage:  python oracle/build_ref.py && python tests/golden/make_golden.py
 """
@@ -162,6 +164,86 @@ def run_dense_case(name):
     return name, n_dl
 
 
+# The at-scale configurations, too large to store: the reference's grid
+# stages on the 256^3 torus (R=0.6, r=0.25, [-1,1]^3, tube 3h) pinned by
+# SHA-256 digests of its exact outputs (grids, tube index list, x*, normals,
+# Jacobian, regularisation factor) and a strided sample of delta and w (they
+# hold cos(), which differs between libm and CUDA in the last bit).
+DIGEST_CASES = {
+    "ref_dirichlet_torus_n256_digest": dict(variant="dirichlet", N=256, wave=20.0, shape="torus", R=0.6, r=0.25,
+                                            stride=97),
+}
+
+
+def digest(a):
+    import hashlib
+    return hashlib.sha256(np.ascontiguousarray(a).tobytes()).hexdigest()
+
+
+def run_digest_case(name):
+    import oracle as O
+    case = DIGEST_CASES[name]
+    ref = O.Reference(case["variant"])
+    N, k = case["N"], case["wave"]
+    d = distance(case, ref.int_l, ref.int_u)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    ref.setup(N, k, d)
+    out = {"d": digest(d)}
+    for nm, g in zip(("gx", "gy", "gz", "mc", "gc"), ref.grids()):
+        out[nm] = digest(g)
+    idx = ref.tube()
+    n = len(idx)
+    out["idx"] = digest(idx.astype(np.int64))
+    tp = ref.tube_points(n)
+    for nm in ("xs", "nrm", "jac", "reg"):
+        out[nm] = digest(tp[nm])
+    st = case["stride"]
+    meta = dict(name=name, N=N, wave=k, int_l=ref.int_l, int_u=ref.int_u, factor=ref.factor,
+                tau_factor=ref.tau_factor, dirichlet=ref.dirichlet, interior=ref.interior, n=n, R=case["R"],
+                r=case["r"], stride=st, flagged=int(tp["flagged"]), sha256=out)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), delta=tp["delta"][::st],
+                        w=tp["w"][::st])
+    return name, n
+
+
+# Benchmark configuration 1 solved by the reference: sphere R=0.5 at the
+# origin on 64^3 over [-1,1]^3, tube 3h, k=5, Dirichlet data of a point
+# source at the origin; the reference's dense matrix (omp_get_Ccomp) and its
+# CompBiCG, run to 1e-13.  The input grid is regenerated by the test
+# (geometry.sphere) and pinned by its digest; the density is stored.
+SOLVE_CASES = {
+    "ref_dirichlet_sphere_n64_solve": dict(variant="dirichlet", N=64, wave=5.0, shape="sphere", radius=0.5,
+                                           center=(0.0, 0.0, 0.0), rhs_kind=0),
+}
+
+
+def run_solve_case(name):
+    import oracle as O
+    case = SOLVE_CASES[name]
+    ref = O.Reference(case["variant"])
+    N, k = case["N"], case["wave"]
+    d = distance(case, ref.int_l, ref.int_u)
+    devnull = os.open(os.devnull, os.O_WRONLY)
+    os.dup2(devnull, 1)
+    ref.setup(N, k, d)
+    idx = ref.tube()
+    n = len(idx)
+    tp = ref.tube_points(n)
+    are, aim = ref.dense(n)
+    orc = O.Oracle()
+    par = ref.params(N, k)
+    b = orc.rhs(par, dict(xs=tp["xs"], nrm=tp["nrm"], w=tp["w"], reg=tp["reg"]), np.zeros(3), case["rhs_kind"])
+    x = ref.compbicg(are, aim, b)
+    del are, aim
+    meta = dict(name=name, N=N, wave=k, int_l=ref.int_l, int_u=ref.int_u, factor=ref.factor,
+                tau_factor=ref.tau_factor, dirichlet=ref.dirichlet, interior=ref.interior, n=n,
+                radius=case["radius"], center=list(case["center"]), rhs_kind=case["rhs_kind"], acc=1e-13,
+                sha256=dict(d=digest(d), idx=digest(idx.astype(np.int64)), b=digest(b)))
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), x=x)
+    return name, n
+
+
 # Godunov upwind |grad phi| (finite_difference3D.c:5-27), the Hamiltonian
 # of the level-set reinitialisation: seeded one-sided derivatives with
 # zeros and both signs mixed in, for signage -1, 0 and +1.
@@ -184,7 +266,8 @@ def run_godunov_case(name):
 def main():
     # One process per case: the reference exits (status 0) on some inputs and
     # keeps per-process statics, so each case gets a fresh, time-limited child.
-    names = sys.argv[1:] or list(CASES) + list(DENSE_CASES) + list(GODUNOV_CASES)
+    names = sys.argv[1:] or (list(CASES) + list(DENSE_CASES) + list(GODUNOV_CASES) + list(DIGEST_CASES) +
+                             list(SOLVE_CASES))
     for name in names:
         out = os.path.join(HERE, name + ".npz")
         if os.path.exists(out):
@@ -203,6 +286,10 @@ if __name__ == "__main__":
             run_dense_case(sys.argv[2])
         elif sys.argv[2] in GODUNOV_CASES:
             run_godunov_case(sys.argv[2])
+        elif sys.argv[2] in DIGEST_CASES:
+            run_digest_case(sys.argv[2])
+        elif sys.argv[2] in SOLVE_CASES:
+            run_solve_case(sys.argv[2])
         else:
             run_case(sys.argv[2])
     else:
