@@ -11,6 +11,7 @@
 // densities of a tile are staged as RB/2 rows of two complex values each.
 #include "hz_internal.cuh"
 #include "sincos64.cuh"
+#include "pair64.cuh"
 #include "bulk_copy.cuh"
 #include "krylov_multi.cuh"
 
@@ -212,6 +213,8 @@ struct ArgsM64 {
     int64_t n;
     int nr;
     double wave, tau, tau2, sg;
+    float kscale;     // k * 2048 / (2 pi), the phase table index in FP32
+    long long tau2b;  // bit pattern of tau^2
     const double4_32a *pos, *nrm;
     const double4_32a *dens;  // [RB/2][n]: (w p_{2q}, w p_{2q+1})
     const double *p_re, *p_im;
@@ -251,8 +254,8 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
     constexpr int T = kT64m;
     extern __shared__ __align__(128) double4_32a smem64[];
     __shared__ alignas(8) uint64_t bar[2];
-    __shared__ double2 tab[kSinTable];
-    fill_sin_table(tab);
+    __shared__ alignas(16) double2 tab[kPhaseTable];
+    fill_phase_table(tab);
     double4_32a *sp[2] = {smem64, smem64 + (2 + RB / 2) * T};
     const double c4 = 1. / (4. * kPi);
     const int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -302,22 +305,25 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
             for (int j = 0; j < cnt; j++) {
                 const double4_32a s_p = P[j], s_n = Nn[j];
                 const double xmy1 = tp.x - s_p.x, xmy2 = tp.y - s_p.y, xmy3 = tp.z - s_p.z;
-                const double r2 = xmy1 * xmy1 + xmy2 * xmy2 + xmy3 * xmy3;
-                bool far = r2 > a.tau2;
-                if (fabs(r2 - a.tau2) <= 1e-12 * a.tau2) far = sqrt(r2) > a.tau;
+                const double r2 = fma(xmy3, xmy3, fma(xmy2, xmy2, xmy1 * xmy1));
+                // near-field test as in sweep_f64.cu: bit patterns, the
+                // reference's arithmetic within 8192 ulps of tau^2
+                const long long rb = __double_as_longlong(r2);
+                bool far = rb > a.tau2b;
+                if ((unsigned long long)(rb - a.tau2b + 8192) <= 16384ull) {
+                    const double r2ref = __dadd_rn(__dadd_rn(__dmul_rn(xmy1, xmy1), __dmul_rn(xmy2, xmy2)),
+                                                   __dmul_rn(xmy3, xmy3));
+                    far = __dsqrt_rn(r2ref) > a.tau;
+                }
                 double vr, vi;
                 if (far) {
-                    const double rec = rsqrt(r2);
-                    const double rho = r2 * rec;
-                    double S, C;
-                    table_sincos(a.wave * rho, tab, S, C);
-                    const double denom = c4 * rec * rec;
-                    const double ct1 = -1. * (a.wave * S + C * rec) * denom;
-                    const double ct2 = (a.wave * C - S * rec) * denom;
-                    const double in = DIR ? (xmy1 * s_n.x + xmy2 * s_n.y + xmy3 * s_n.z)
-                                          : (xmy1 * tn.x + xmy2 * tn.y + xmy3 * tn.z);
-                    vr = a.sg * ct1 * in;
-                    vi = a.sg * ct2 * in;
+                    double ur, ui, y2;
+                    far_factor64(r2, a.wave, a.kscale, tab, ur, ui, y2);
+                    const double in = DIR ? fma(xmy3, s_n.z, fma(xmy2, s_n.y, xmy1 * s_n.x))
+                                          : fma(xmy3, tn.z, fma(xmy2, tn.y, xmy1 * tn.x));
+                    const double f = (a.sg * c4) * (in * y2);
+                    vr = ur * f;
+                    vi = ui * f;
                 } else {
                     vr = DIR ? s_p.w : tp.w;
                     vi = 0.0;
@@ -368,6 +374,11 @@ int launch_m64(const SweepConst &c, const Rec64 &r64, int nr, const double *pr, 
                double *qi, void *scratch, cudaStream_t s)
 {
     constexpr int smem = (int)smem_m64<RB>();
+    if (!(c.wave * c.extent <= kMaxPhase64)) {
+        set_error("FP64 multi-RHS sweep: k * domain diagonal = %g exceeds the phase reduction's range (%g)",
+                  c.wave * c.extent, kMaxPhase64);
+        return HZ_ERR_ARG;
+    }
     HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<RB, false>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     HZ_CHECK_CUDA(cudaFuncSetAttribute(sweepm64_kernel<RB, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem));
     double4_32a *dens = static_cast<double4_32a *>(scratch);
@@ -379,6 +390,8 @@ int launch_m64(const SweepConst &c, const Rec64 &r64, int nr, const double *pr, 
     a.wave = c.wave;
     a.tau = c.tau;
     a.tau2 = c.tau * c.tau;
+    a.tau2b = __builtin_bit_cast(long long, a.tau2);
+    a.kscale = (float)(c.wave * (kPhaseTable / (2.0 * kPi)));
     a.sg = (c.interior == 1) ? -1.0 : 1.0;
     a.pos = r64.pos;
     a.nrm = r64.nrm;
