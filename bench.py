@@ -78,6 +78,8 @@ def parse():
                     help="--solve: timed plain-FP64 BiCG iterations (the full FP64 solve time is this "
                          "per-iteration time x the iteration count; --fp64-full runs it to tolerance)")
     ap.add_argument("--fp64-full", action="store_true")
+    ap.add_argument("--fp64-tol", type=float, default=0.0,
+                    help="--solve --fp64-full: tolerance of the FP64 solve (default: the smallest --tol)")
     ap.add_argument("--fp64-solve-iters", type=int, default=0,
                     help="--solve: FP64 BiCG iteration count of a complete solve, for the extrapolated FP64 time")
     ap.add_argument("--method", choices=["bicg", "gmres"], nargs="*", default=["bicg", "gmres"],
@@ -496,13 +498,13 @@ def run_solve(a, local):
                             gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
                 out["runs"].append(info)
                 sols[(meth, tol)] = x
-        # plain FP64 BiCG: per-iteration time (and, with --fp64-full, the whole solve)
+        # plain FP64 BiCG: the whole solve with --fp64-full, else its per-iteration time
         if a.save:
             os.makedirs(a.save, exist_ok=True)
             for (meth, t), x in sols.items():
                 np.save(os.path.join(a.save, "x_%s_%s_%g.npy" % (a.shape, meth, t)), x)
         if a.fp64_full:
-            tol = min(a.tol)
+            tol = a.fp64_tol or min(a.tol)
             x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=tol, maxit=2000)
             info.update(precision="f64", tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
             out["runs"].append(info)
@@ -510,18 +512,33 @@ def run_solve(a, local):
             out["f64_solve_s"] = info["seconds"]
             if a.save:
                 np.save(os.path.join(a.save, "x_%s_f64_%g.npy" % (a.shape, tol)), x64)
-            # off-surface field at 100 seeded receivers on the sphere r = 0.9
-            rx = G.random_sphere_points(100, 0.9, seed=7)
-            u64 = op.evaluate(rx, x64, hz.DOUBLE_LAYER)
+            sols[("f64 bicg", tol)] = x64
+        # errors of every solution against the FP64 solve and against the
+        # tightest refined solve (an FP64-accurate solution when its FP64
+        # residual is far below the others' tolerances): density (max-norm
+        # and 2-norm relative) and off-surface field at 100 seeded receivers
+        # on the sphere r = 0.9
+        refs = {}
+        if a.fp64_full:
+            refs["f64 bicg %g" % tol] = x64
+        tight = min(a.tol)
+        if len(a.tol) > 1:
+            for meth in a.method:
+                refs["%s %g" % (meth, tight)] = sols[(meth, tight)]
+        rx = G.random_sphere_points(100, 0.9, seed=7)
+        for rname, xr in refs.items():
+            ur = op.evaluate(rx, xr, hz.DOUBLE_LAYER)
+            errs = {}
             for (meth, t), x in sols.items():
-                out.setdefault("rel_err_vs_f64", {})["%s %g" % (meth, t)] = float(
-                    np.max(np.abs(x - x64)) / np.max(np.abs(x64)))
-                out.setdefault("rel_err2_vs_f64", {})["%s %g" % (meth, t)] = float(
-                    np.linalg.norm(x - x64) / np.linalg.norm(x64))
+                key = "%s %g" % (meth, t)
+                if key == rname:
+                    continue
                 u = op.evaluate(rx, x, hz.DOUBLE_LAYER)
-                out.setdefault("field_rel_err_vs_f64", {})["%s %g" % (meth, t)] = float(
-                    np.max(np.abs(u - u64)) / np.max(np.abs(u64)))
-        elif a.fp64_iters > 0:
+                errs[key] = {"density_max": float(np.max(np.abs(x - xr)) / np.max(np.abs(xr))),
+                             "density_2": float(np.linalg.norm(x - xr) / np.linalg.norm(xr)),
+                             "field_max": float(np.max(np.abs(u - ur)) / np.max(np.abs(ur)))}
+            out.setdefault("rel_err_vs", {})[rname] = errs
+        if not a.fp64_full and a.fp64_iters > 0:
             x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=1e-300, maxit=a.fp64_iters,
                                  stagnation=0)
             per_it = info["seconds"] / max(1, info["iterations"])
