@@ -142,6 +142,7 @@ SIGNATURES = {
     "hz_matvec_pair": ([_vp, C.c_int, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_matvec_multi": ([_vp, C.c_int, C.c_int, _vp, _vp, _vp, _vp, C.c_int], C.c_int),
     "hz_solve": ([_vp, C.POINTER(SolveOpts), _vp, _vp, _vp, _vp, C.c_int, C.POINTER(SolveInfo)], C.c_int),
+    "hz_residual_history": ([_vp, _vp, C.c_int, C.POINTER(C.c_int)], C.c_int),
     "hz_solve_opts_default": ([C.POINTER(SolveOpts)], None),
     "hz_solve_multi": ([_vp, C.POINTER(SolveOpts), C.c_int, _vp, _vp, _vp, _vp, C.c_int, C.POINTER(SolveInfo),
                         _vp], C.c_int),
@@ -391,6 +392,16 @@ class Operator:
         rc = load().hz_solve(self.h, C.byref(opts), _ptr(br), _ptr(bi), _ptr(xr), _ptr(xi), HZ_HOST, C.byref(info))
         _check(rc)
         return xr + 1j * xi, info.as_dict()
+
+    def residual_history(self):
+        """Relative residual after each Krylov iteration of the last solve
+        (BiCG/BiCGSTAB; inner FP32 solves one after another when refined)."""
+        cnt = C.c_int()
+        _check(load().hz_residual_history(self.h, None, 0, C.byref(cnt)))
+        out = np.empty(cnt.value)
+        if cnt.value:
+            _check(load().hz_residual_history(self.h, _ptr(out), cnt.value, C.byref(cnt)))
+        return out
 
     def solve_multi(self, B, opts=None, **kw):
         """Solve for every row of B ([nrhs][n] complex); returns X, info, resid."""

@@ -290,6 +290,7 @@ struct hz_solver_state {
     DevBuf mvec, mscratch, mpack;  // multi right-hand side staging, sweep scratch, packed columns
     DevBuf gwork, gsmall, gx;  // GMRES basis, Hessenberg partials, inner solution
     DevBuf xbest;              // refinement: best iterate so far (re/im)
+    std::vector<double> history;  // per-iteration residuals of the last hz_solve (BiCG/BiCGSTAB)
 };
 
 namespace {
@@ -1057,6 +1058,7 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
             return HZ_OK;
         }
     }
+    st->history.clear();
     if (o.precision != HZ_PREC_F32_REFINED && o.method == HZ_GMRES) {
         MatrixFreeOp Af(op, o.precision);
         AdjointOp Aa(Af);
@@ -1077,6 +1079,7 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         AdjointOp Aa(Af);
         LinOp &A = adjoint ? static_cast<LinOp &>(Aa) : static_cast<LinOp &>(Af);
         HZ_TRY(st->outer.solve(A, o.method, b0, b1, o.tol, o.maxit, o.stagnation != 0, true, s, iters, resid, status));
+        st->history = st->outer.history;
         HZ_CHECK_CUDA(cudaMemcpyAsync(x0, st->outer.re(Krylov::X), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         HZ_CHECK_CUDA(cudaMemcpyAsync(x1, st->outer.im(Krylov::X), n * sizeof(double), cudaMemcpyDeviceToDevice, s));
         inf.iterations = iters;
@@ -1089,6 +1092,7 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
     }
     // FP64 iterative refinement around FP32 inner solves.
     HZ_TRY(st->inner.reserve(n));
+    st->history.clear();
     MatrixFreeOp A32f(op, HZ_PREC_F32), A64f(op, HZ_PREC_F64);
     AdjointOp A32a(A32f), A64a(A64f);
     LinOp &A32 = adjoint ? static_cast<LinOp &>(A32a) : static_cast<LinOp &>(A32f);
@@ -1132,6 +1136,7 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         } else {
             HZ_TRY(st->inner.solve(A32, o.method, q0, q1, itol, o.maxit, o.stagnation != 0, true, s, it, ires, ist,
                                    kInnerStall));
+            st->history.insert(st->history.end(), st->inner.history.begin(), st->inner.history.end());
             products += 2LL * it;
             e0 = st->inner.re(Krylov::X);
             e1 = st->inner.im(Krylov::X);
@@ -1238,6 +1243,19 @@ int hz_solve(hz_operator *op, const hz_solve_opts *opts_in, const double *b_re, 
         else set_error("hz_solve: solver stopped early (status %d)", status);
         return status;
     }
+    return HZ_OK;
+}
+
+int hz_residual_history(hz_operator *op, double *out, int cap, int *count)
+{
+    if (!op || !count || cap < 0 || (cap > 0 && !out)) {
+        set_error("hz_residual_history: bad arguments");
+        return HZ_ERR_ARG;
+    }
+    const std::vector<double> &h = op->solver->history;
+    const int m = (int)h.size();
+    for (int i = 0; i < m && i < cap; i++) out[i] = h[i];
+    *count = m;
     return HZ_OK;
 }
 

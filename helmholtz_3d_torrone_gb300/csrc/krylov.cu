@@ -452,6 +452,7 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
     const int vb = vec_blocks(n);
     iters = 0;
     status = HZ_OK;
+    history.clear();
     if (method == HZ_BICG) {
         bicg_init_kernel<<<vb, 256, 0, s>>>(n, b_re, b_im, re(X), im(X), re(R), im(R), re(RT), im(RT), re(P),
                                             im(P), re(PT), im(PT));
@@ -526,6 +527,7 @@ int Krylov::solve(LinOp &A, int method, const double *b_re, const double *b_im, 
         iters = it;
         const double preerr = host_err[1];
         err = host_err[0];
+        history.push_back(err);
         const int st = (int)host_err[2];
         if (err < tol) break;
         if (err != err) {

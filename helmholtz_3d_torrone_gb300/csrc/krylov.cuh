@@ -1,6 +1,8 @@
 // krylov.cuh -- device Krylov solvers over an abstract linear operator.
 #pragma once
 
+#include <vector>
+
 #include "hz_internal.cuh"
 
 namespace hz {
@@ -67,6 +69,7 @@ class Krylov {
     double *re(int v);
     double *im(int v);
     void invalidate_graph() { graph_key = 0; }
+    std::vector<double> history;  // relative residual after each iteration of the last solve
 
   private:
     int bicg_iteration(LinOp &A, cudaStream_t s);

@@ -230,6 +230,14 @@ HZ_API int hz_solve(hz_operator *op, const hz_solve_opts *opts, const double *b_
              double *x_re, double *x_im, int where, hz_solve_info *info);
 HZ_API void hz_solve_opts_default(hz_solve_opts *o);
 
+/* Relative residual after each Krylov iteration of the operator's last
+ * hz_solve with BiCG or BiCGSTAB (the FP32 inner solves one after another
+ * for refined solves, each relative to its own right-hand side; empty after
+ * GMRES).  Copies min(cap, count) values into out and sets *count.  No
+ * counterpart in the reference, which prints only the final residual
+ * (BICGSTAB.c:310). */
+HZ_API int hz_residual_history(hz_operator *op, double *out, int cap, int *count);
+
 /* Receiver misfit and its gradients by the adjoint method.
  * J = sum_m |u(x_m) - t_m|^2 with u = E sigma (layer as in hz_eval) and
  * A sigma = b.  One forward solve, one adjoint solve A^H lambda = E^H r
