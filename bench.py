@@ -495,7 +495,8 @@ def run_solve(a, local):
                 x, info = op.solve(b, method=mid, precision=hz.PREC_F32_REFINED, tol=tol, inner_tol=a.inner_tol,
                                    restart=a.restart, max_outer=8)
                 info.update(precision="f32+f64-refine", method=meth, tol=tol,
-                            gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
+                            gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9,
+                            history=[float("%.3e" % v) for v in op.residual_history()])
                 out["runs"].append(info)
                 sols[(meth, tol)] = x
         # plain FP64 BiCG: the whole solve with --fp64-full, else its per-iteration time
@@ -506,7 +507,8 @@ def run_solve(a, local):
         if a.fp64_full:
             tol = a.fp64_tol or min(a.tol)
             x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=tol, maxit=2000)
-            info.update(precision="f64", tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9)
+            info.update(precision="f64", tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9,
+                        history=[float("%.3e" % v) for v in op.residual_history()])
             out["runs"].append(info)
             out["f64_solve_iterations"] = info["iterations"]
             out["f64_solve_s"] = info["seconds"]
