@@ -7,27 +7,30 @@ R=0.6, r=0.25 sampled as its analytic signed distance on a 256^3 grid over
 (double-layer) formulation with point-source data from (0.6, 0, 0).
 
 The headline ``value`` is the wall time of one complete solve of that
-system to an FP64 relative residual below 1e-6: FP32 inner BiCG solves
-(one fused FP32 pair sweep producing A p and A^H pt per iteration, tile-local
-origins, phase k rho passed to the SFU sin/cos) inside FP64 iterative
-refinement whose residual b - A x comes from the FP64 sweep.  It replaces
-the reference's parallel_BiCGcomplex (large3Dexample2.c:2954-3514).  ``e2e``
-is the same solve through the public C ABI with host buffers (H2D of b, D2H
-of x inside the timed region).
+system to an FP64 relative residual below 1e-6: FP32 inner GMRES(120)
+solves (one FP32 pair sweep per iteration, tile-local origins, phase k rho
+passed to the SFU sin/cos) inside FP64 iterative refinement whose residual
+b - A x comes from the FP64 pair sweep.  It replaces the reference's
+parallel_BiCGcomplex (large3Dexample2.c:2954-3514).  ``e2e`` is the same
+solve through the public C ABI with host buffers (H2D of b, D2H of x inside
+the timed region).
 
-Beside it: the plain FP64 GPU solve (measured seconds per FP64 BiCG
-iteration x the iteration count of a complete FP64 solve of this workload,
-measured once with ``--solve --fp64-full`` and recorded in FP64_SOLVE_ITERS),
-and the pair rate of the inner iteration (``--steps`` timed iterations, L2
-flushed between them) with its roofline.
+Beside it: the plain FP64 GPU solve with the same method (measured seconds
+of one FP64 product x the product count of a complete FP64 GMRES(120)
+solve of this workload, measured once with ``--solve --fp64-full`` and
+recorded in FP64_SOLVE_ITERS), the roofline of the FP64 sweep (the kernel
+that takes most of the solve's time: two FP64 residual products), and the
+FP32 sweep's rate and roofline over ``--steps`` timed inner iterations (L2
+flushed between them).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
 ``--impl reference`` measures the reference's own CPU pair evaluation
 (omp_get_Ccomp + its complex multiply-add) on the host cores for the same
-workload (oracle/cpu_rate.py) and prints the extrapolated time of its FP64
-BiCG solve, FP64_SOLVE_ITERS x 2 n^2 / rate; with several ranks only rank 0
-runs it.
+workload (oracle/cpu_rate.py) and prints a lower bound of its solve time,
+FP64_SOLVE_ITERS x n^2 / rate: the FP64 product count of the GMRES solve
+(the reference's BiCG needs two products per iteration); with several ranks
+only rank 0 runs it.
 """
 import argparse
 import csv
@@ -49,15 +52,22 @@ METRIC = "256³ solve time & Gpair/s: FP32+FP64-refine vs plain FP64 GPU at 1e-6
 FLOPS_PER_PAIR = 40  # reference pair formula, large3Dexample2.c:4471-4550
 SOLVE_TOL = 1e-6     # FP64 relative residual of the timed solve
 INNER_TOL = 1e-7     # tightest inner FP32 tolerance (the first step solves to SOLVE_TOL / 4)
-# Iterations of the complete plain-FP64 BiCG solve of this workload to
-# SOLVE_TOL, measured on a GB300 with --solve --fp64-full (None: not yet
-# measured; the FP64 and CPU solve times are then not extrapolated).
+RESTART = 120        # GMRES basis size (no restart within these solves)
+# Products (iterations) of the complete plain-FP64 GMRES(120) solve of this
+# workload to SOLVE_TOL, measured on a GB300 with --solve --fp64-full
+# (None: not yet measured; the FP64 and CPU solve times are then not given).
 FP64_SOLVE_ITERS = None
 # DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
 # 22.36 MB measured by ncu on the 128^3 torus (n = 145,272), scaled by n to
 # n = 581,420.  The sweep reads every record once from DRAM and the tiles
 # from L2, so traffic grows in proportion to n.
 SWEEP32_TRAFFIC = 22.36e6 * 581420 / 145272
+# The same for one A p launch and for one FP64 sweep: records, densities and
+# the result once (48 + 16 + 16 B per point for the FP32 sweep's split target
+# record, source record, input and output; 64 + 32 + 32 B for the FP64 one),
+# source tiles from L2.  Scaled to n = 581,420 until a capture replaces them.
+SWEEP32_TRAFFIC_A = 80.0 * 581420
+SWEEP64_TRAFFIC = 16.5e6 * 581420 / 145272  # ncu DRAM read of the FP64 sweep at 128^3, scaled by n
 
 
 def parse():
@@ -78,6 +88,8 @@ def parse():
                     help="--solve: timed plain-FP64 BiCG iterations (the full FP64 solve time is this "
                          "per-iteration time x the iteration count; --fp64-full runs it to tolerance)")
     ap.add_argument("--fp64-full", action="store_true")
+    ap.add_argument("--fp64-method", choices=["bicg", "gmres"], default="gmres",
+                    help="--solve --fp64-full: method of the FP64 solve")
     ap.add_argument("--fp64-tol", type=float, default=0.0,
                     help="--solve --fp64-full: tolerance of the FP64 solve (default: the smallest --tol)")
     ap.add_argument("--fp64-solve-iters", type=int, default=0,
@@ -145,20 +157,21 @@ def workload_desc(N, wave, n):
 
 
 def solve_desc():
-    return {"tol": SOLVE_TOL, "inner_tol_floor": INNER_TOL, "method": "bicg",
-            "value": "seconds of one complete solve to FP64 relative residual < tol: FP32 inner BiCG (fused A p + "
-                     "A^H pt sweep per iteration) inside FP64 iterative refinement (residual b - A x from the FP64 "
+    return {"tol": SOLVE_TOL, "inner_tol_floor": INNER_TOL, "method": "gmres(%d)" % RESTART,
+            "value": "seconds of one complete solve to FP64 relative residual < tol: FP32 inner GMRES (one FP32 "
+                     "sweep A p per iteration) inside FP64 iterative refinement (residual b - A x from the FP64 "
                      "sweep); b resident in HBM, CUDA events on the operator's stream, run once after the step loop",
-            "step": "one iteration of that inner BiCG (fused FP32 sweep over all 2 n^2 pairs + FP64 vector "
-                    "updates), L2 flushed between steps by a 256 MB device write; the steps give the pair rate"}
+            "step": "one iteration of that inner GMRES (FP32 sweep over all n^2 pairs + FP64 Gram-Schmidt), L2 "
+                    "flushed between steps by a 256 MB device write; the steps give the FP32 pair rate"}
 
 
 def cpu_solve_seconds(pair_rate, n):
-    """Extrapolated time of the reference's FP64 BiCG solve on the host cores:
-    FP64_SOLVE_ITERS iterations x 2 n^2 pair evaluations / the measured rate."""
+    """Lower bound of the reference's FP64 solve time on the host cores:
+    FP64_SOLVE_ITERS products x n^2 pair evaluations / the measured rate
+    (its BiCG evaluates two products per iteration)."""
     if not FP64_SOLVE_ITERS or not pair_rate:
         return None
-    return FP64_SOLVE_ITERS * 2.0 * n * n / pair_rate
+    return FP64_SOLVE_ITERS * 1.0 * n * n / pair_rate
 
 
 def cpu_rate(N, wave, impl, steps, warmup, step_seconds, timeout=900):
@@ -240,10 +253,10 @@ def run_reference(a, rank, world):
         "impl": "reference", "metric": METRIC, "value": solve_s, "unit": "s", "n_gpus": a.gpus,
         "steps": a.steps, "warmup": a.warmup, "ms_per_step": 1e3 * total_s / len(rates),
         "higher_is_better": False, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": dict(workload_desc(a.N, a.wave, n), tol=SOLVE_TOL, method="bicg (CompBiCG, FP64)",
-                       value="extrapolated FP64 BiCG solve time on the host cores: %s iterations (of the complete "
-                             "FP64 GPU solve of this workload) x 2 n^2 pairs / the measured pair rate"
-                             % FP64_SOLVE_ITERS,
+        "config": dict(workload_desc(a.N, a.wave, n), tol=SOLVE_TOL, method="FP64 (the reference's pair formula)",
+                       value="lower bound of the FP64 solve time on the host cores: %s products (of the complete "
+                             "FP64 GMRES(%d) GPU solve of this workload; the reference's BiCG needs two per "
+                             "iteration) x n^2 pairs / the measured pair rate" % (FP64_SOLVE_ITERS, RESTART),
                        step="reference pair evaluation + complex MAC over a bounded block of target rows x all n "
                             "sources"),
         "pair_rate_gpair_s": rate / 1e9,
@@ -295,9 +308,10 @@ def run_gb300(a, rank, world, local):
     x_re = torch.empty(n, dtype=torch.float64, device=dev)
     x_im = torch.empty(n, dtype=torch.float64, device=dev)
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
-    step_opts = hz.solve_opts(method=hz.BICG, precision=hz.PREC_F32, tol=1e-300, maxit=1, stagnation=0)
-    solve_opts = hz.solve_opts(method=hz.BICG, precision=hz.PREC_F32_REFINED, tol=SOLVE_TOL, inner_tol=INNER_TOL,
-                               maxit=2000, max_outer=8)
+    step_opts = hz.solve_opts(method=hz.GMRES, precision=hz.PREC_F32, tol=1e-300, maxit=1, stagnation=0,
+                              restart=RESTART)
+    solve_opts = hz.solve_opts(method=hz.GMRES, precision=hz.PREC_F32_REFINED, tol=SOLVE_TOL, inner_tol=INNER_TOL,
+                               maxit=2000, max_outer=8, restart=RESTART)
     info = hz.SolveInfo()
 
     def call(opts, where, br, bi, xr, xi):
@@ -337,7 +351,7 @@ def run_gb300(a, rank, world, local):
     sweep_ms, sweep_launches = op.sweep_timing(-1)
     op.sweep_timing(0)
     elapsed = max_over_ranks(dist, max(dev_s, 1e-9), dev)
-    pairs_step = 2 * n * n
+    pairs_step = n * n
     step_rate = job_rate(pairs_step, a.steps, world, elapsed)
 
     # ---------------- the metric: one complete refined solve, b resident in HBM
@@ -374,25 +388,31 @@ def run_gb300(a, rank, world, local):
     x_dev = x_re.cpu().numpy() + 1j * x_im.cpu().numpy()
     e2e_vs_dev = float(np.max(np.abs(x_host - x_dev)) / np.max(np.abs(x_dev)))
 
-    # ---------------- plain FP64 GPU comparator: seconds per FP64 BiCG iteration
+    # ---------------- plain FP64 GPU comparator: one FP64 product (the FP64
+    # sweep, CUDA events on the operator's stream), also the roofline of the
+    # kernel that takes most of the refined solve's time
     f64 = None
     if a.fp64_iters > 0:
-        f64_opts = hz.solve_opts(method=hz.BICG, precision=hz.PREC_F64, tol=1e-300, maxit=a.fp64_iters,
-                                 stagnation=0)
+        y_re = torch.empty(n, dtype=torch.float64, device=dev)
+        y_im = torch.empty(n, dtype=torch.float64, device=dev)
         ev4 = torch.cuda.Event(enable_timing=True)
         ev5 = torch.cuda.Event(enable_timing=True)
         ev4.record(stream)
-        finfo = call(f64_opts, hz.HZ_DEVICE, *dptr)
+        for _ in range(a.fp64_iters):
+            rc = L.hz_matvec(op.h, hz.PREC_F64, 0, x_re.data_ptr(), x_im.data_ptr(), y_re.data_ptr(),
+                             y_im.data_ptr(), hz.HZ_DEVICE)
+            if rc != 0:
+                raise hz.HzError(rc, L.hz_last_error().decode())
         ev5.record(stream)
         torch.cuda.synchronize()
-        per_it = ev4.elapsed_time(ev5) / 1e3 / max(1, finfo["iterations"])
-        f64 = {"seconds_per_iteration": per_it, "iterations_timed": finfo["iterations"],
-               "gpair_per_s": 2.0 * n * n / per_it / 1e9,
-               "solve_iterations": FP64_SOLVE_ITERS,
-               "solve_s_extrapolated": per_it * FP64_SOLVE_ITERS if FP64_SOLVE_ITERS else None,
-               "how": "measured seconds per FP64 BiCG iteration (fused FP64 A p + A^H pt sweep + FP64 vector "
-                      "updates, CUDA events) x the iteration count of a complete FP64 solve of this workload "
-                      "to the same tol, measured once (bench.py --solve --fp64-full)"}
+        per_prod = ev4.elapsed_time(ev5) / 1e3 / a.fp64_iters
+        f64 = {"seconds_per_product": per_prod, "products_timed": a.fp64_iters,
+               "gpair_per_s": float(n) * n / per_prod / 1e9,
+               "solve_products": FP64_SOLVE_ITERS,
+               "solve_s_extrapolated": per_prod * FP64_SOLVE_ITERS if FP64_SOLVE_ITERS else None,
+               "how": "measured seconds of one FP64 product (sweep64_kernel, CUDA events) x the product count of "
+                      "a complete FP64 GMRES(%d) solve of this workload to the same tol, measured once (bench.py "
+                      "--solve --fp64-full); GMRES adds only FP64 Gram-Schmidt (milliseconds) per product" % RESTART}
         if f64["solve_s_extrapolated"]:
             f64["speedup_refined_vs_f64"] = f64["solve_s_extrapolated"] / solve_s
 
@@ -401,6 +421,15 @@ def run_gb300(a, rank, world, local):
         return 0
     avg_sweep_s = (sweep_ms / sweep_launches) / 1e3 if sweep_launches else None
     achieved = pairs_step * FLOPS_PER_PAIR / avg_sweep_s / 1e12 if avg_sweep_s else None
+    roof64 = None
+    if f64:
+        a64 = float(n) * n * FLOPS_PER_PAIR / f64["seconds_per_product"] / 1e12
+        roof64 = {"bound": "fp64", "kernel": "sweep64_kernel (A x, the FP64 refinement residual)",
+                  "achieved": a64, "peak": fp64_peak, "unit": "TFLOP/s", "frac": a64 / fp64_peak,
+                  "traffic": SWEEP64_TRAFFIC, "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": n * n,
+                  "avg_launch_ms": f64["seconds_per_product"] * 1e3, "launches_timed": a.fp64_iters,
+                  "peak_source": "FP64 DFMA chains measured live on this GPU (hz_measure_fma_peaks)",
+                  "share_of_solve": 2 * f64["seconds_per_product"] / solve_s if sinfo["outer"] >= 2 else None}
     keep = ("iterations", "outer", "resid_f64", "converged", "pair_evals", "steps", "step_iters",
             "step_inner_tol", "step_resid")
     line = {
@@ -419,14 +448,14 @@ def run_gb300(a, rank, world, local):
         "fp64_gpu": f64,
         "step_rate": {"value": step_rate, "unit": "Gpair/s", "pairs_per_step": pairs_step, "wall_s": wall},
         "gpu_launches": launches,
-        "roofline": {"bound": "fp32", "kernel": "sweep32_kernel (fused A p + A^H pt)",
-                     "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
-                     "frac": (achieved / fp32_peak) if achieved else None, "traffic": SWEEP32_TRAFFIC,
-                     "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": pairs_step,
-                     "avg_launch_ms": avg_sweep_s * 1e3 if avg_sweep_s else None,
-                     "launches_timed": sweep_launches,
-                     "peak_source": "FP32 FFMA chains measured live on this GPU (hz_measure_fma_peaks)",
-                     "fp64_peak_tflops": fp64_peak},
+        "roofline": roof64,
+        "roofline_fp32": {"bound": "fp32", "kernel": "sweep32_kernel (A p, the inner GMRES product)",
+                          "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                          "frac": (achieved / fp32_peak) if achieved else None, "traffic": SWEEP32_TRAFFIC_A,
+                          "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": pairs_step,
+                          "avg_launch_ms": avg_sweep_s * 1e3 if avg_sweep_s else None,
+                          "launches_timed": sweep_launches,
+                          "peak_source": "FP32 FFMA chains measured live on this GPU (hz_measure_fma_peaks)"},
         "clocks": clk,
     }
     op.close()
@@ -506,15 +535,16 @@ def run_solve(a, local):
                 np.save(os.path.join(a.save, "x_%s_%s_%g.npy" % (a.shape, meth, t)), x)
         if a.fp64_full:
             tol = a.fp64_tol or min(a.tol)
-            x64, info = op.solve(b, method=hz.BICG, precision=hz.PREC_F64, tol=tol, maxit=2000)
-            info.update(precision="f64", tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9,
+            fm = hz.GMRES if a.fp64_method == "gmres" else hz.BICG
+            x64, info = op.solve(b, method=fm, precision=hz.PREC_F64, tol=tol, maxit=2000, restart=a.restart)
+            info.update(precision="f64", method=a.fp64_method, tol=tol, gpair_per_s=info["pair_evals"] / info["seconds"] / 1e9,
                         history=[float("%.3e" % v) for v in op.residual_history()])
             out["runs"].append(info)
             out["f64_solve_iterations"] = info["iterations"]
             out["f64_solve_s"] = info["seconds"]
             if a.save:
                 np.save(os.path.join(a.save, "x_%s_f64_%g.npy" % (a.shape, tol)), x64)
-            sols[("f64 bicg", tol)] = x64
+            sols[("f64 " + a.fp64_method, tol)] = x64
         # errors of every solution against the FP64 solve and against the
         # tightest refined solve (an FP64-accurate solution when its FP64
         # residual is far below the others' tolerances): density (max-norm
@@ -522,7 +552,7 @@ def run_solve(a, local):
         # on the sphere r = 0.9
         refs = {}
         if a.fp64_full:
-            refs["f64 bicg %g" % tol] = x64
+            refs["f64 %s %g" % (a.fp64_method, tol)] = x64
         tight = min(a.tol)
         if len(a.tol) > 1:
             for meth in a.method:

@@ -1110,13 +1110,24 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
     int outer = 0;
     long long products = 0;
     const bool gm = o.method == HZ_GMRES;
-    if (gm) HZ_TRY(st->gx.ensure((size_t)n * 2 * sizeof(double)));
-    // the best iterate (lowest FP64 residual) is kept: a step that does not
-    // lower the residual ends the refinement and the best iterate is returned
-    HZ_TRY(st->xbest.ensure((size_t)n * 2 * sizeof(double)));
-    double *xb0 = st->xbest.as<double>(), *xb1 = xb0 + n;
+    HZ_TRY(st->gx.ensure((size_t)n * 2 * sizeof(double)));
+    // The best iterate (lowest FP64 residual) and its residual are kept.  A
+    // step that does not lower the residual goes back to them; the step is
+    // then repeated once with GMRES, whose inner residual cannot grow (a
+    // BiCG inner solve can stall on a rough residual), and a second failure
+    // ends the refinement with the best iterate.
+    HZ_TRY(st->xbest.ensure((size_t)n * 4 * sizeof(double)));
+    double *xb0 = st->xbest.as<double>(), *xb1 = xb0 + n, *rb0 = xb0 + 2 * n, *rb1 = xb0 + 3 * n;
+    const int restart = (o.restart >= 2 && o.restart <= 127) ? o.restart : 40;
     double best = res;
-    bool stalled = false;
+    bool stalled = false, retry = false;
+    auto copy2 = [&](double *d0, double *d1, const double *s0, const double *s1) -> int {
+        HZ_CHECK_CUDA(cudaMemcpyAsync(d0, s0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        HZ_CHECK_CUDA(cudaMemcpyAsync(d1, s1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        return HZ_OK;
+    };
+    HZ_TRY(copy2(xb0, xb1, x0, x1));
+    HZ_TRY(copy2(rb0, rb1, r0, r1));
     while (normb > 0 && res >= o.tol && outer < o.max_outer) {
         outer++;
         // inner right-hand side r / ||r|| (into q)
@@ -1125,11 +1136,11 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         double ires = 0.0;
         const double itol = refine_inner_tol(o, res);
         const double *e0, *e1;
-        if (gm) {
+        if (gm || retry) {
             int prods = 0;
             double *g0 = st->gx.as<double>(), *g1 = g0 + n;
-            HZ_TRY(gmres_solve(A32, n, o.restart, q0, q1, g0, g1, itol, o.maxit, kInnerStall, st->gwork, st->gsmall,
-                               s, it, ires, prods));
+            HZ_TRY(gmres_solve(A32, n, restart, q0, q1, g0, g1, itol, o.maxit, kInnerStall, st->gwork, st->gsmall, s,
+                               it, ires, prods));
             products += prods;
             e0 = g0;
             e1 = g1;
@@ -1154,29 +1165,30 @@ static int solve_device(hz_operator *op, const hz_solve_opts &o, bool adjoint, c
         A64.iteration_done(false);
         res = nr / normb;
         if (inf.steps < HZ_MAX_STEPS) {
-            inf.step_iters[inf.steps] = it;
+            inf.step_iters[inf.steps] = (gm || retry) ? -it : it;
             inf.step_inner_tol[inf.steps] = itol;
             inf.step_resid[inf.steps] = res;
             inf.steps++;
         }
         if (!(res < best)) {
             // no progress (or a non-finite residual): back to the best iterate
-            if (outer > 1) {
-                HZ_CHECK_CUDA(cudaMemcpyAsync(x0, xb0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-                HZ_CHECK_CUDA(cudaMemcpyAsync(x1, xb1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-            } else {
-                HZ_CHECK_CUDA(cudaMemsetAsync(x0, 0, n * sizeof(double), s));
-                HZ_CHECK_CUDA(cudaMemsetAsync(x1, 0, n * sizeof(double), s));
-            }
+            HZ_TRY(copy2(x0, x1, xb0, xb1));
+            HZ_TRY(copy2(r0, r1, rb0, rb1));
             res = best;
+            nr = best * normb;
+            if (!gm && !retry) {
+                retry = true;
+                continue;
+            }
             stalled = true;
             if (ist == HZ_ERR_BREAKDOWN) status = HZ_ERR_BREAKDOWN;
             break;
         }
         best = res;
+        retry = false;
         if (res >= o.tol && outer < o.max_outer) {
-            HZ_CHECK_CUDA(cudaMemcpyAsync(xb0, x0, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
-            HZ_CHECK_CUDA(cudaMemcpyAsync(xb1, x1, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+            HZ_TRY(copy2(xb0, xb1, x0, x1));
+            HZ_TRY(copy2(rb0, rb1, r0, r1));
         }
     }
     inf.iterations = iters;

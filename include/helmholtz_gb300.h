@@ -107,9 +107,10 @@ typedef struct hz_solve_opts {
                           to fall.  An inner solve also stops once it has run
                           max(30, iterations to its last new minimum) iterations
                           without a new minimum, and returns its best iterate    */
-    int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap; refinement also
-                          stops, keeping its best iterate, when a step does not
-                          lower the FP64 residual                                      */
+    int max_outer;     /* HZ_PREC_F32_REFINED: refinement step cap.  A step that does
+                          not lower the FP64 residual is undone and repeated once
+                          with an inner GMRES(restart); a second such step ends
+                          the refinement with the best iterate                     */
     int stagnation;    /* 1: also stop when |delta(||r||/||b||)| < 1e-3 tol (reference) */
     int restart;       /* HZ_GMRES: Krylov basis size before a restart (2..127)         */
 } hz_solve_opts;
@@ -133,7 +134,8 @@ typedef struct hz_solve_info {
                              returns after its last iteration                     */
     /* refined solves: the first HZ_MAX_STEPS refinement steps, one entry each */
     int steps;                           /* entries filled (min(outer, HZ_MAX_STEPS)) */
-    int step_iters[HZ_MAX_STEPS];        /* inner Krylov iterations of the step       */
+    int step_iters[HZ_MAX_STEPS];        /* inner Krylov iterations of the step
+                                            (negative: the step ran GMRES)            */
     double step_inner_tol[HZ_MAX_STEPS]; /* inner tolerance the step solved to        */
     double step_resid[HZ_MAX_STEPS];     /* FP64 relative residual after the step     */
 } hz_solve_info;

@@ -20,7 +20,11 @@ hz_shape_gradient).
   projections).  J is only piecewise smooth in phi (a pair crossing the
   near-field radius, an upwind or limiter branch flipping), so a node is
   kept where the quotients with steps 1e-6 and 2e-6 agree to 1e-5 of the
-  largest quotient; the GPU gradient matches there to 1e-5 of it.
+  largest quotient.  Where no branch lies near the node the GPU gradient
+  equals the quotient to about 1e-8 of the largest one; a branch within a
+  step of the node bends both quotients alike, so it passes that screen
+  while the adjoint (the derivative on one side) differs by up to a few
+  1e-5.  The test asks for 1e-6 on at least 8 nodes and 1e-4 on all.
 """
 import numpy as np
 import pytest
@@ -160,5 +164,6 @@ def test_dJ_dphi_vs_reference_solve(hz, oracle):
     smooth = np.abs(q1 - q2) <= 1e-5 * scale
     assert np.count_nonzero(smooth) >= 8, (q1, q2)
     gq = np.array([gphi[q] for q in nodes])
-    err = np.abs(gq - q1)[smooth]
-    assert np.max(err) <= 1e-5 * scale, (gq[smooth], q1[smooth])
+    err = np.abs(gq - q1)[smooth] / scale
+    assert np.count_nonzero(err <= 1e-6) >= 8, (err, gq[smooth], q1[smooth])
+    assert np.max(err) <= 1e-4, (err, gq[smooth], q1[smooth])
