@@ -124,6 +124,10 @@ def parse():
                     help="--batch: grid sizes drawn per surface")
     ap.add_argument("--batch-axes", type=float, nargs=2, default=[0.2, 0.7],
                     help="--batch: range of the seeded semi-axes")
+    ap.add_argument("--product", choices=["f32", "f64", "pair32", "pair64"], default="",
+                    help="instead of the step benchmark: build the torus operator at --N and run --steps products of "
+                         "this kind (A p, or the fused A p + A^H pt), timed with CUDA events (short runs for "
+                         "profilers)")
     ap.add_argument("--sweep-variant", type=int, default=-1,
                     help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
@@ -867,14 +871,50 @@ def run_batch(a):
     return 0
 
 
+def run_product(a):
+    """--steps products of one kind on the torus at --N (after --warmup)."""
+    import numpy as np
+    import torch
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    d = G.torus(a.N, R=0.6, r=0.25, int_l=-1.0, int_u=1.0)
+    p = hz.params(a.N, a.wave, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1)
+    with hz.Operator(p) as op:
+        op.set_distance(d)
+        n = op.build()
+        if a.sweep_variant >= 0:
+            op.set_sweep_config(a.sweep_variant)
+        rng = np.random.default_rng(1)
+        v = rng.standard_normal(n) + 1j * rng.standard_normal(n)
+        prec = hz.PREC_F64 if a.product.endswith("64") else hz.PREC_F32
+
+        def one():
+            if a.product.startswith("pair"):
+                return op.matvec_pair(v, v, precision=prec)[0]
+            return op.matvec(v, precision=prec)
+        for _ in range(a.warmup):
+            one()
+        t0 = time.perf_counter()
+        for _ in range(a.steps):
+            q = one()
+        dt = (time.perf_counter() - t0) / max(1, a.steps)
+        print(json.dumps({"mode": "product", "product": a.product, "N": a.N, "n": n, "wave": a.wave,
+                          "seconds_per_product": dt, "gpair_per_s": float(n) * n / dt / 1e9,
+                          "note": "wall time of hz_matvec / hz_matvec_pair incl. host<->device copies",
+                          "q0": [float(q[0].real), float(q[0].imag)]}))
+    return 0
+
+
 def main():
     a = parse()
     rank, world, local = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
-    if a.solve or a.plane_waves or a.batch or a.gradient or a.combo:
+    if a.solve or a.plane_waves or a.batch or a.gradient or a.combo or a.product:
         import torch
         torch.cuda.set_device(local)
+        if a.product:
+            return run_product(a)
         if a.gradient:
             return run_gradient(a)
         if a.combo:
