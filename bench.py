@@ -114,6 +114,8 @@ def parse():
                          "grid node, dJ/dg, dJ/dk by adjoint solves) with central-difference checks")
     ap.add_argument("--products-only", action="store_true",
                     help="--plane-waves: time the multi right-hand-side products only, no solves")
+    ap.add_argument("--single-waves", type=int, default=4,
+                    help="--plane-waves: waves also solved one at a time (per method) for the comparison")
     ap.add_argument("--plane-waves", type=int, default=0,
                     help="instead of the step benchmark: solve this many incident plane waves (Fibonacci-sphere "
                          "directions) on the torus with the multi right-hand-side solver and report the times")
@@ -636,17 +638,20 @@ def run_plane_waves(a):
         # solves: all R in lockstep (FP32 + FP64 refinement) vs one refined BiCGSTAB solve per field
         X, info, res = op.solve_multi(B, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
         out["multi_solve"] = dict(info, max_resid=float(np.max(res)))
-        nsingle = min(R, 4)
-        t0 = time.perf_counter()
-        errs = []
-        for r in range(nsingle):
-            x, i1 = op.solve(B[r], method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
-            errs.append(float(np.max(np.abs(x - X[r])) / np.max(np.abs(x))))
-        t_one = (time.perf_counter() - t0) / nsingle
-        out["single_solves"] = {"seconds_per_field": t_one, "fields_timed": nsingle,
-                                "seconds_for_all_extrapolated": t_one * R,
-                                "max_rel_diff_vs_multi": max(errs)}
-        out["multi_solve_speedup_vs_single_extrapolated"] = t_one * R / info["seconds"]
+        nsingle = min(R, a.single_waves)
+        for meth, name in ((hz.BICGSTAB, "bicgstab"), (hz.GMRES, "gmres")):
+            t0 = time.perf_counter()
+            errs = []
+            for r in range(nsingle):
+                x, i1 = op.solve(B[r], method=meth, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5,
+                                 restart=a.restart)
+                errs.append(float(np.max(np.abs(x - X[r])) / np.max(np.abs(x))))
+            t_one = (time.perf_counter() - t0) / nsingle
+            out["single_solves_" + name] = {"seconds_per_field": t_one, "fields_timed": nsingle,
+                                            "seconds_for_all_extrapolated": t_one * R,
+                                            "max_rel_diff_vs_multi": max(errs),
+                                            "method": "refined %s, one wave at a time" % name}
+            out["multi_solve_speedup_vs_single_%s_extrapolated" % name] = t_one * R / info["seconds"]
     print(json.dumps(out))
     sys.stdout.flush()
     return 0
