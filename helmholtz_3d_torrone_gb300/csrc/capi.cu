@@ -142,8 +142,9 @@ struct MatrixFreeOp final : LinOp {
         if (precision == HZ_PREC_F64)
             return sweep_f64(c, rec64(op), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re, qt_im,
                              op->scratch.as<double2>(), s, e0, e1);
+        const int cfg = (mode == SWEEP_PAIR || op->sweep_cfg_a < 0) ? op->sweep_cfg : op->sweep_cfg_a;
         return sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), mode, p_re, p_im, pt_re, pt_im, q_re, q_im, qt_re,
-                         qt_im, op->dens32.as<float4>(), s, e0, e1, op->sweep_cfg);
+                         qt_im, op->dens32.as<float4>(), s, e0, e1, cfg);
     }
     void capture_begin() override { op->timer.next = 0; }
     void capture_end() override
@@ -163,7 +164,7 @@ struct MatrixFreeOp final : LinOp {
     uint64_t key() const override
     {
         return ((uint64_t)(uintptr_t)op << 8) ^ (uint64_t)(precision * 16 + op->sweep_cfg) ^
-               ((uint64_t)op->phase_mode << 6) ^ 1ull;
+               ((uint64_t)op->phase_mode << 6) ^ ((uint64_t)(op->sweep_cfg_a + 1) << 32) ^ 1ull;
     }
 };
 
@@ -656,31 +657,40 @@ int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep)
     HZ_CHECK_CUDA(cudaEventCreate(&e0));
     HZ_CHECK_CUDA(cudaEventCreate(&e1));
     const SweepConst c = sweep_const(op);
-    int best = 0;
-    float best_ms = 1e30f;
+    // the fused pass (BiCG) and the single-product pass (GMRES, BiCGSTAB,
+    // the refinement's inner products) are timed and chosen separately
+    int best = 0, best_a = 0;
+    float best_ms = 1e30f, best_a_ms = 1e30f;
     int rc = HZ_OK;
-    for (int cfg = 0; cfg < sweep32_num_configs() && rc == HZ_OK; cfg++) {
-        float ms_min = 1e30f;
-        for (int rep = 0; rep < 2 && rc == HZ_OK; rep++) {
-            rc = sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), SWEEP_PAIR, io, io + n, io + 2 * n, io + 3 * n,
-                           io + 4 * n, io + 5 * n, io + 6 * n, io + 7 * n, op->dens32.as<float4>(), s, e0, e1, cfg);
-            if (rc == HZ_OK && cudaEventSynchronize(e1) == cudaSuccess) {
-                float ms = 0.f;
-                cudaEventElapsedTime(&ms, e0, e1);
-                if (ms < ms_min) ms_min = ms;
+    for (int mode : {SWEEP_PAIR, SWEEP_A}) {
+        for (int cfg = 0; cfg < sweep32_num_configs() && rc == HZ_OK; cfg++) {
+            float ms_min = 1e30f;
+            for (int rep = 0; rep < 2 && rc == HZ_OK; rep++) {
+                rc = sweep_f32(c, op->r32, op->pos64.as<double4_32a>(), mode, io, io + n, io + 2 * n, io + 3 * n,
+                               io + 4 * n, io + 5 * n, io + 6 * n, io + 7 * n, op->dens32.as<float4>(), s, e0, e1,
+                               cfg);
+                if (rc == HZ_OK && cudaEventSynchronize(e1) == cudaSuccess) {
+                    float ms = 0.f;
+                    cudaEventElapsedTime(&ms, e0, e1);
+                    if (ms < ms_min) ms_min = ms;
+                }
             }
-        }
-        if (ms_min < best_ms) {
-            best_ms = ms_min;
-            best = cfg;
+            if (mode == SWEEP_PAIR && ms_min < best_ms) {
+                best_ms = ms_min;
+                best = cfg;
+            } else if (mode == SWEEP_A && ms_min < best_a_ms) {
+                best_a_ms = ms_min;
+                best_a = cfg;
+            }
         }
     }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
     if (rc != HZ_OK) return rc;
     HZ_TRY(check_device_error(op, "hz_autotune"));
-    if (best != op->sweep_cfg) {
+    if (best != op->sweep_cfg || best_a != op->sweep_cfg_a) {
         op->sweep_cfg = best;
+        op->sweep_cfg_a = best_a;
         op->solver->outer.invalidate_graph();
         op->solver->inner.invalidate_graph();
     }
@@ -695,8 +705,9 @@ int hz_set_sweep_config(hz_operator *op, int cfg)
         set_error("hz_set_sweep_config: config must be in [0, %d)", sweep32_num_configs());
         return HZ_ERR_ARG;
     }
-    if (cfg != op->sweep_cfg) {
+    if (cfg != op->sweep_cfg || op->sweep_cfg_a != -1) {
         op->sweep_cfg = cfg;
+        op->sweep_cfg_a = -1;
         op->solver->outer.invalidate_graph();
         op->solver->inner.invalidate_graph();
     }

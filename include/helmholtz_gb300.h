@@ -165,9 +165,11 @@ HZ_API int hz_build(hz_operator *op, int64_t *n);
 HZ_API int64_t hz_tube_size(const hz_operator *op);
 
 /* Autotuner: times every compiled variant of the FP32 pair sweep (block
- * shape x targets per thread) on this operator's tube and keeps the
- * fastest for all later FP32 sweeps.  Returns the chosen variant and its
- * time for one fused A p + A^H pt sweep.  hz_set_sweep_config forces one. */
+ * shape x targets per thread) on this operator's tube, once as the fused
+ * A p + A^H pt pass (BiCG) and once as a single product (GMRES, BiCGSTAB),
+ * and keeps the fastest of each for all later FP32 sweeps.  Returns the
+ * fused pass's variant and time.  hz_set_sweep_config forces one variant
+ * for both. */
 HZ_API int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep);
 HZ_API int hz_set_sweep_config(hz_operator *op, int cfg);
 
