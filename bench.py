@@ -54,9 +54,11 @@ SOLVE_TOL = 1e-6     # FP64 relative residual of the timed solve
 INNER_TOL = 1e-7     # tightest inner FP32 tolerance (the first step solves to SOLVE_TOL / 4)
 RESTART = 120        # GMRES basis size (no restart within these solves)
 # Products (iterations) of the complete plain-FP64 GMRES(120) solve of this
-# workload to SOLVE_TOL, measured on a GB300 with --solve --fp64-full
-# (None: not yet measured; the FP64 and CPU solve times are then not given).
-FP64_SOLVE_ITERS = None
+# workload to SOLVE_TOL: 67, measured on a GB300 with
+# bench.py --solve --N 256 --tol 1e-6 1e-11 --method gmres bicg --restart 120
+#          --fp64-full --fp64-tol 1e-6 --fp64-method gmres
+# (1,708 s, FP64 residual 8.4e-7).
+FP64_SOLVE_ITERS = 67
 # DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
 # 22.36 MB measured by ncu on the 128^3 torus (n = 145,272), scaled by n to
 # n = 581,420.  The sweep reads every record once from DRAM and the tiles
@@ -68,6 +70,7 @@ SWEEP32_TRAFFIC = 22.36e6 * 581420 / 145272
 # source tiles from L2.  Scaled to n = 581,420 until a capture replaces them.
 SWEEP32_TRAFFIC_A = 80.0 * 581420
 SWEEP64_TRAFFIC = 16.5e6 * 581420 / 145272  # ncu DRAM read of the FP64 sweep at 128^3, scaled by n
+FP64_OPS_PER_PAIR = 41.5  # FP64 instructions per pair of the A-mode FP64 sweep (ncu, 128^3 torus)
 
 
 def parse():
@@ -432,6 +435,11 @@ def run_gb300(a, rank, world, local):
         a64 = float(n) * n * FLOPS_PER_PAIR / f64["seconds_per_product"] / 1e12
         roof64 = {"bound": "fp64", "kernel": "sweep64_kernel (A x, the FP64 refinement residual)",
                   "achieved": a64, "peak": fp64_peak, "unit": "TFLOP/s", "frac": a64 / fp64_peak,
+                  "fp64_ops_per_pair": FP64_OPS_PER_PAIR,
+                  "pipe_frac": float(n) * n * FP64_OPS_PER_PAIR / f64["seconds_per_product"] / (fp64_peak * 0.5e12),
+                  "note": "frac counts the reference formula's 40 flops per pair against the DFMA peak (2 flops per "
+                          "instruction); pipe_frac counts the FP64 instructions the kernel executes (ncu) against "
+                          "the pipe's instruction rate (peak / 2)",
                   "traffic": SWEEP64_TRAFFIC, "flops_per_pair": FLOPS_PER_PAIR, "pairs_per_launch": n * n,
                   "avg_launch_ms": f64["seconds_per_product"] * 1e3, "launches_timed": a.fp64_iters,
                   "peak_source": "FP64 DFMA chains measured live on this GPU (hz_measure_fma_peaks)",
