@@ -95,6 +95,7 @@ Rec64 rec64(hz_operator *op)
     Rec64 r;
     r.pos = op->pos64.as<double4_32a>();
     r.nrm = op->nrm64.as<double4_32a>();
+    r.posk = op->posk64.ptr ? op->posk64.as<double4_32a>() : nullptr;
     return r;
 }
 
@@ -622,6 +623,12 @@ int hz_build(hz_operator *op, int64_t *n_out)
                      op->w.as<double>(), op->pos64.as<double4_32a>(), op->nrm64.as<double4_32a>(), op->err.as<unsigned>(), s,
                      op->dreg.as<double>()));
     HZ_TRY(check_device_error(op, "hz_build"));
+    if (op->p.wave >= 1.0) {
+        HZ_TRY(op->posk64.ensure(nn * sizeof(double4_32a)));
+        HZ_TRY(scale_records64(n, op->p.wave, op->pos64.as<double4_32a>(), op->posk64.as<double4_32a>(), s));
+    } else {
+        op->posk64.release();
+    }
     HZ_TRY(build_records32(op, sweep32_reg_scale(op->p.interior)));
     // scratch for the FP64 sweep densities (double4_32a per point) and staging
     HZ_TRY(op->scratch.ensure(nn * sizeof(double4_32a) + 256));

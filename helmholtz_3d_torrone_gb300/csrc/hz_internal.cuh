@@ -74,6 +74,7 @@ struct DevBuf {
 struct Rec64 {
     double4_32a *pos;  // x*, y*, z*, reg
     double4_32a *nrm;  // nx, ny, nz, w
+    const double4_32a *posk = nullptr;  // k x*, k y*, k z*, reg (optional: the scaled FP64 sweep)
 };
 
 // Tile geometry of the FP32 sweep.
@@ -209,6 +210,8 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
               const double *pt_re, const double *pt_im, double *q_re, double *q_im, double *qt_re,
               double *qt_im, double2 *scratch, cudaStream_t s, cudaEvent_t ev0 = nullptr,
               cudaEvent_t ev1 = nullptr);
+// posk[i] = (k x, k y, k z, reg) of pos[i]: the FP64 sweep's scaled records.
+int scale_records64(int64_t n, double k, const double4_32a *pos, double4_32a *posk, cudaStream_t s);
 // sweep_f32.cu
 int sweep_f32(const SweepConst &c, const Rec32 &r, const double4_32a *pos64, int mode,
               const double *p_re, const double *p_im, const double *pt_re, const double *pt_im,
@@ -268,6 +271,7 @@ struct hz_operator {
     int64_t n = 0;
     hz::DevBuf idx, xs, nrm, delta, jac, reg, w, dreg;
     hz::DevBuf pos64, nrm64;
+    hz::DevBuf posk64;  // pos64 with the coordinates scaled by k (FP64 sweep)
     // FP32 sweep records
     hz::Rec32 r32{};
     hz::DevBuf perm, pos32, nrm32, origin32, tpos32, split32, nearmask32, partial32;

@@ -37,10 +37,11 @@ namespace {
 struct Args64 {
     int64_t n;
     double wave, tau, tau2;
-    float kscale;       // k * 2048 / (2 pi): the phase table index in FP32
-    long long tau2b;    // bit pattern of tau^2
-    double inv_scale;  // 4 pi sg: the near-field value times this cancels the density prescale
+    float kscale;       // k * 2048 / (2 pi) (2048 / (2 pi) on scaled coordinates): the phase table index
+    long long tau2b;    // bit pattern of tau^2 ((k tau)^2 on scaled coordinates)
+    double inv_scale;  // 4 pi sg (/ k^2 scaled): the near-field value times this cancels the density prescale
     const double4_32a *pos, *nrm;
+    const double4_32a *posu;  // unscaled positions (the near-field tie test of the scaled sweep)
     const double4_32a *dens;  // (w_s p_re, w_s p_im, pt_re, pt_im)
     const double *p_re, *p_im, *pt_re, *pt_im;
     double *q_re, *q_im, *qt_re, *qt_im;
@@ -73,23 +74,37 @@ __global__ void prep64_kernel(int64_t n, const double4_32a *__restrict__ nrm, co
 
 constexpr double kPi64 = 3.14159265358979323846264338328;
 
-// One (target, source) pair added to acc = (A re, A im, A^H re, A^H im).
-template <int MODE, bool DIR>
+// The reference's near-field decision sqrt(rho^2) > tau, rho^2 summed
+// without fused multiply-adds, on unscaled coordinate differences.
+__device__ __forceinline__ bool far_exact(double dx, double dy, double dz, double tau)
+{
+    const double r2ref = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
+    return __dsqrt_rn(r2ref) > tau;
+}
+
+// One (target t, source s) pair added to acc = (A re, A im, A^H re, A^H im).
+// SCALED: positions are k x, so the differences, rho^2 and the projection
+// carry factors of k (the densities carry the k^2 of the entry).
+template <int MODE, bool DIR, bool SCALED>
 __device__ __forceinline__ void pair64(const Args64 &a, const double2 *tab, const double4_32a &tp,
                                        const double4_32a &tn, const double4_32a &sp, const double4_32a &sn,
-                                       const double4_32a &sd, double *acc)
+                                       const double4_32a &sd, int64_t t, int64_t s, double *acc)
 {
     const double dx = tp.x - sp.x, dy = tp.y - sp.y, dz = tp.z - sp.z;
     const double r2 = fma(dz, dz, fma(dy, dy, dx * dx));
     const long long rb = __double_as_longlong(r2);
     bool far = rb > a.tau2b;
     if ((unsigned long long)(rb - a.tau2b + kTieUlps) <= (unsigned long long)(2 * kTieUlps)) {
-        const double r2ref = __dadd_rn(__dadd_rn(__dmul_rn(dx, dx), __dmul_rn(dy, dy)), __dmul_rn(dz, dz));
-        far = __dsqrt_rn(r2ref) > a.tau;
+        if (SCALED) {
+            const double4_32a u = a.posu[t], v = a.posu[s];
+            far = far_exact(u.x - v.x, u.y - v.y, u.z - v.z, a.tau);
+        } else {
+            far = far_exact(dx, dy, dz, a.tau);
+        }
     }
     if (far) {
         double ur, ui, y2;
-        far_factor64(r2, a.wave, a.kscale, tab, ur, ui, y2);
+        far_factor64<SCALED>(r2, a.wave, a.kscale, tab, ur, ui, y2);
         if (MODE & SWEEP_A) {
             const double in = DIR ? fma(dz, sn.z, fma(dy, sn.y, dx * sn.x)) : fma(dz, tn.z, fma(dy, tn.y, dx * tn.x));
             const double f = in * y2;
@@ -119,7 +134,7 @@ __device__ __forceinline__ void pair64(const Args64 &a, const double2 *tab, cons
     }
 }
 
-template <int MODE, bool DIR>
+template <int MODE, bool DIR, bool SCALED>
 __global__ void __launch_bounds__(kThreads64, 4) sweep64_kernel(Args64 a)
 {
     constexpr int T = kSrc64;
@@ -181,7 +196,9 @@ __global__ void __launch_bounds__(kThreads64, 4) sweep64_kernel(Args64 a)
                 const double4_32a sn_ = sn[buf][j];
                 const double4_32a sd_ = sd[buf][j];
 #pragma unroll
-                for (int g = 0; g < kTgt64; g++) pair64<MODE, DIR>(a, tab, tp[g], tn[g], sp_, sn_, sd_, acc[g]);
+                for (int g = 0; g < kTgt64; g++)
+                    pair64<MODE, DIR, SCALED>(a, tab, tp[g], tn[g], sp_, sn_, sd_, t0 + (int64_t)g * blockDim.x,
+                                              base + j, acc[g]);
             }
         }
         __syncthreads();
@@ -206,13 +223,31 @@ __global__ void __launch_bounds__(kThreads64, 4) sweep64_kernel(Args64 a)
     }
 }
 
-template <int MODE>
+template <int MODE, bool SCALED>
 void launch64(const Args64 &a, bool dir, cudaStream_t s)
 {
     const int per_block = kThreads64 * kTgt64;
     const unsigned blocks = (unsigned)((a.n + per_block - 1) / per_block);
-    if (dir) sweep64_kernel<MODE, true><<<blocks, kThreads64, 0, s>>>(a);
-    else sweep64_kernel<MODE, false><<<blocks, kThreads64, 0, s>>>(a);
+    if (dir) sweep64_kernel<MODE, true, SCALED><<<blocks, kThreads64, 0, s>>>(a);
+    else sweep64_kernel<MODE, false, SCALED><<<blocks, kThreads64, 0, s>>>(a);
+}
+
+template <bool SCALED>
+void launch64_mode(const Args64 &a, int mode, bool dir, cudaStream_t s)
+{
+    if (mode == SWEEP_PAIR) launch64<SWEEP_PAIR, SCALED>(a, dir, s);
+    else if (mode == SWEEP_A) launch64<SWEEP_A, SCALED>(a, dir, s);
+    else launch64<SWEEP_AH, SCALED>(a, dir, s);
+}
+
+// posk[i] = (k x*, k y*, k z*, reg): the records of the scaled sweep.
+__global__ void scale_records64_kernel(int64_t n, double k, const double4_32a *__restrict__ pos,
+                                       double4_32a *__restrict__ posk)
+{
+    for (int64_t i = blockIdx.x * (int64_t)blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+        const double4_32a p = pos[i];
+        posk[i] = make_double4_32a(k * p.x, k * p.y, k * p.z, p.w);
+    }
 }
 
 }  // namespace
@@ -230,6 +265,27 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
     }
     double4_32a *dens = reinterpret_cast<double4_32a *>(scratch);
     const bool useA = (mode & SWEEP_A) != 0, useH = (mode & SWEEP_AH) != 0;
+    // Coordinates scaled by k (records built by scale_records64) save three
+    // FP64 operations per pair; below k = 1 (and for records without a
+    // scaled copy) the unscaled sweep runs.
+    const bool scaled = r.posk != nullptr && c.wave >= 1.0;
+    const double sg = (c.interior == 1) ? -1.0 : 1.0;
+    const double k2 = scaled ? c.wave * c.wave : 1.0;
+    Args64 a;
+    a.n = c.n;
+    a.wave = c.wave;
+    a.tau = c.tau;
+    a.tau2 = scaled ? (c.wave * c.tau) * (c.wave * c.tau) : c.tau * c.tau;
+    a.tau2b = __builtin_bit_cast(long long, a.tau2);
+    a.kscale = (float)((scaled ? 1.0 : c.wave) * (kPhaseTable / (2.0 * kPi64)));
+    a.inv_scale = sg * (4.0 * kPi64) / k2;
+    a.pos = scaled ? r.posk : r.pos;
+    a.posu = r.pos;
+    a.nrm = r.nrm;
+    a.dens = dens;
+    a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
+    a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
+    a.err = c.err;
     {
         int dev = 0, sms = 152;
         cudaGetDevice(&dev);
@@ -238,29 +294,24 @@ int sweep_f64(const SweepConst &c, const Rec64 &r, int mode, const double *p_re,
         if (b > sms * 8) b = sms * 8;
         prep64_kernel<<<(unsigned)b, 256, 0, s>>>(c.n, r.nrm, useA ? p_re : nullptr, useA ? p_im : nullptr,
                                                   useH ? pt_re : nullptr, useH ? pt_im : nullptr,
-                                                  ((c.interior == 1) ? -1.0 : 1.0) / (4.0 * kPi64), dens);
+                                                  sg * k2 / (4.0 * kPi64), dens);
         HZ_CHECK_LAUNCH();
     }
-    Args64 a;
-    a.n = c.n;
-    a.wave = c.wave;
-    a.tau = c.tau;
-    a.tau2 = c.tau * c.tau;
-    a.tau2b = (long long)__builtin_bit_cast(long long, a.tau2);
-    a.kscale = (float)(c.wave * (kPhaseTable / (2.0 * kPi64)));
-    a.inv_scale = ((c.interior == 1) ? -1.0 : 1.0) * (4.0 * kPi64);
-    a.pos = r.pos;
-    a.nrm = r.nrm;
-    a.dens = dens;
-    a.p_re = p_re; a.p_im = p_im; a.pt_re = pt_re; a.pt_im = pt_im;
-    a.q_re = q_re; a.q_im = q_im; a.qt_re = qt_re; a.qt_im = qt_im;
-    a.err = c.err;
     if (ev0) HZ_CHECK_CUDA(record_timing_event(ev0, s));
-    if (mode == SWEEP_PAIR) launch64<SWEEP_PAIR>(a, c.dirichlet != 0, s);
-    else if (mode == SWEEP_A) launch64<SWEEP_A>(a, c.dirichlet != 0, s);
-    else launch64<SWEEP_AH>(a, c.dirichlet != 0, s);
+    if (scaled) launch64_mode<true>(a, mode, c.dirichlet != 0, s);
+    else launch64_mode<false>(a, mode, c.dirichlet != 0, s);
     HZ_CHECK_LAUNCH();
     if (ev1) HZ_CHECK_CUDA(record_timing_event(ev1, s));
+    return HZ_OK;
+}
+
+int scale_records64(int64_t n, double k, const double4_32a *pos, double4_32a *posk, cudaStream_t s)
+{
+    if (n <= 0) return HZ_OK;
+    long long b = (n + 255) / 256;
+    if (b > 4096) b = 4096;
+    scale_records64_kernel<<<(unsigned)b, 256, 0, s>>>(n, k, pos, posk);
+    HZ_CHECK_LAUNCH();
     return HZ_OK;
 }
 

@@ -318,7 +318,7 @@ __global__ void __launch_bounds__(kT64m) sweepm64_kernel(ArgsM64 a)
                 double vr, vi;
                 if (far) {
                     double ur, ui, y2;
-                    far_factor64(r2, a.wave, a.kscale, tab, ur, ui, y2);
+                    far_factor64<false>(r2, a.wave, a.kscale, tab, ur, ui, y2);
                     const double in = DIR ? fma(xmy3, s_n.z, fma(xmy2, s_n.y, xmy1 * s_n.x))
                                           : fma(xmy3, tn.z, fma(xmy2, tn.y, xmy1 * tn.x));
                     const double f = (a.sg * c4) * (in * y2);
