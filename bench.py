@@ -370,10 +370,12 @@ def run_gb300(a, rank, world, local):
     barrier()
     ev2 = torch.cuda.Event(enable_timing=True)
     ev3 = torch.cuda.Event(enable_timing=True)
+    solve_launches0 = hz.kernel_launches()
     ev2.record(stream)
     t1 = time.perf_counter()
     sinfo = call(solve_opts, hz.HZ_DEVICE, *dptr)
     ev3.record(stream)
+    solve_launches = hz.kernel_launches() - solve_launches0
     torch.cuda.synchronize()
     solve_wall = time.perf_counter() - t1
     solve_s = max_over_ranks(dist, ev2.elapsed_time(ev3) / 1e3, dev)
@@ -461,7 +463,8 @@ def run_gb300(a, rank, world, local):
                 "how": "hz_solve with pinned host b and x (H2D of b, D2H of x inside the timed region), wall clock"},
         "fp64_gpu": f64,
         "step_rate": {"value": step_rate, "unit": "Gpair/s", "pairs_per_step": pairs_step, "wall_s": wall},
-        "gpu_launches": launches,
+        "gpu_launches": solve_launches,
+        "step_launches": launches,
         "roofline": roof64,
         "roofline_fp32": {"bound": "fp32", "kernel": "sweep32_kernel (A p, the inner GMRES product)",
                           "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
