@@ -117,6 +117,8 @@ def parse():
                          "grid node, dJ/dg, dJ/dk by adjoint solves) with central-difference checks")
     ap.add_argument("--products-only", action="store_true",
                     help="--plane-waves: time the multi right-hand-side products only, no solves")
+    ap.add_argument("--multi-method", choices=["gmres", "bicgstab"], default="gmres",
+                    help="--plane-waves: lockstep method of the multi right-hand-side solve")
     ap.add_argument("--single-waves", type=int, default=4,
                     help="--plane-waves: waves also solved one at a time (per method) for the comparison")
     ap.add_argument("--plane-waves", type=int, default=0,
@@ -647,8 +649,10 @@ def run_plane_waves(a):
             sys.stdout.flush()
             return 0
         # solves: all R in lockstep (FP32 + FP64 refinement) vs one refined BiCGSTAB solve per field
-        X, info, res = op.solve_multi(B, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5)
-        out["multi_solve"] = dict(info, max_resid=float(np.max(res)))
+        mm = hz.GMRES if a.multi_method == "gmres" else hz.BICGSTAB
+        X, info, res = op.solve_multi(B, method=mm, precision=hz.PREC_F32_REFINED, tol=a.tol[0], inner_tol=1e-5,
+                                      restart=a.restart)
+        out["multi_solve"] = dict(info, max_resid=float(np.max(res)), method=a.multi_method)
         nsingle = min(R, a.single_waves)
         for meth, name in ((hz.BICGSTAB, "bicgstab"), (hz.GMRES, "gmres")):
             t0 = time.perf_counter()

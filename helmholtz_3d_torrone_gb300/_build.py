@@ -32,6 +32,7 @@ UNITS = {
     "krylov_multi.cu": [],
     "krylov.cu": [],
     "gmres.cu": [],
+    "gmres_multi.cu": [],
     "evaluate.cu": [],
     "adjoint.cu": [],
     "combo.cu": [],

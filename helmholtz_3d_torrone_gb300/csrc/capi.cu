@@ -291,6 +291,7 @@ struct hz_solver_state {
     DevBuf small;
     DevBuf mvec, mscratch, mpack;  // multi right-hand side staging, sweep scratch, packed columns
     DevBuf gwork, gsmall, gx;  // GMRES basis, Hessenberg partials, inner solution
+    DevBuf mgwork, mgsmall, mgx;  // lockstep multi right-hand-side GMRES: basis, partials, inner solutions
     DevBuf xbest;              // refinement: best iterate so far (re/im)
     std::vector<double> history;  // per-iteration residuals of the last hz_solve (BiCG/BiCGSTAB)
 };
@@ -904,10 +905,12 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
     hz_solve_opts o;
     if (opts_in) o = *opts_in;
     else hz_solve_opts_default(&o);
-    if (nrhs < 1 || !(o.tol > 0) || o.maxit < 1 || o.precision < HZ_PREC_F64 || o.precision > HZ_PREC_F32_REFINED) {
+    if (nrhs < 1 || !(o.tol > 0) || o.maxit < 1 || o.precision < HZ_PREC_F64 || o.precision > HZ_PREC_F32_REFINED ||
+        (o.method == HZ_GMRES && (o.restart < 2 || o.restart > 127))) {
         set_error("hz_solve_multi: bad arguments");
         return HZ_ERR_ARG;
     }
+    const bool gm = o.method == HZ_GMRES;
     HZ_CHECK_CUDA(cudaSetDevice(op->device));
     cudaStream_t s = op->stream;
     hz_solver_state *st = op->solver;
@@ -932,9 +935,16 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
     long long pairs = 0;
     if (o.precision != HZ_PREC_F32_REFINED) {
         MultiMatrixFreeOp A(op, o.precision, &st->mscratch, &st->mpack);
-        HZ_TRY(st->multi.solve(A, B0, B1, o.tol, o.maxit, o.stagnation != 0, s, iters, res));
-        HZ_CHECK_CUDA(cudaMemcpyAsync(X0, st->multi.re(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
-        HZ_CHECK_CUDA(cudaMemcpyAsync(X1, st->multi.im(KrylovMulti::X), tot * sizeof(double), cudaMemcpyDeviceToDevice, s));
+        if (gm) {
+            HZ_TRY(gmres_multi_solve(A, n, nrhs, o.restart, B0, B1, X0, X1, o.tol, o.maxit, 0, st->mgwork, st->mgsmall,
+                                     s, iters, res));
+        } else {
+            HZ_TRY(st->multi.solve(A, B0, B1, o.tol, o.maxit, o.stagnation != 0, s, iters, res));
+            HZ_CHECK_CUDA(cudaMemcpyAsync(X0, st->multi.re(KrylovMulti::X), tot * sizeof(double),
+                                          cudaMemcpyDeviceToDevice, s));
+            HZ_CHECK_CUDA(cudaMemcpyAsync(X1, st->multi.im(KrylovMulti::X), tot * sizeof(double),
+                                          cudaMemcpyDeviceToDevice, s));
+        }
         pairs = A.pairs;
     } else {
         // FP64 iterative refinement of every column still above tol:
@@ -974,11 +984,19 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
             int it = 0;
             std::vector<double> ires;
             const double itol = refine_inner_tol(o, worst());
-            HZ_TRY(st->multi.solve(A32, Q0, Q1, itol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStall));
+            const double *E0 = st->multi.re(KrylovMulti::X), *E1 = st->multi.im(KrylovMulti::X);
+            if (gm) {
+                HZ_TRY(st->mgx.ensure(2 * tot * sizeof(double)));
+                double *G0 = st->mgx.as<double>(), *G1 = G0 + tot;
+                HZ_TRY(gmres_multi_solve(A32, n, nrhs, o.restart, Q0, Q1, G0, G1, itol, o.maxit, kInnerStall,
+                                         st->mgwork, st->mgsmall, s, it, ires));
+                E0 = G0;
+                E1 = G1;
+            } else {
+                HZ_TRY(st->multi.solve(A32, Q0, Q1, itol, o.maxit, o.stagnation != 0, s, it, ires, kInnerStall));
+            }
             iters += it;
-            for (int r : open)
-                HZ_TRY(vec_axpy(n, nr[r], st->multi.re(KrylovMulti::X) + r * n, st->multi.im(KrylovMulti::X) + r * n,
-                                X0 + r * n, X1 + r * n, s));
+            for (int r : open) HZ_TRY(vec_axpy(n, nr[r], E0 + r * n, E1 + r * n, X0 + r * n, X1 + r * n, s));
             HZ_TRY(A64.restrict_to(open, s));
             HZ_TRY(A64.apply(nrhs, X0, X1, Q0, Q1, s));
             for (int r : open) {

@@ -56,6 +56,14 @@ class KrylovMulti {
     int graph_flags = 0;
 };
 
+// gmres_multi.cu: lockstep restarted GMRES(m) over R right-hand sides ([R][n]
+// device arrays); x = 0 start; stall as in KrylovMulti::solve.  resid gets
+// each column's final residual estimate, col_iters its iterations.
+size_t gmres_multi_work_bytes(int64_t n, int R, int m);
+int gmres_multi_solve(MultiOp &A, int64_t n, int R, int m, const double *b_re, const double *b_im, double *x_re,
+                      double *x_im, double tol, int maxit, int stall, DevBuf &work, DevBuf &small, cudaStream_t s,
+                      int &iters, std::vector<double> &resid, std::vector<int> *col_iters = nullptr);
+
 // sweep_multi.cu
 // kernel passes (one evaluation of every pair each) for nrhs columns
 long long multi_rhs_passes(int precision, int nrhs);

@@ -214,10 +214,12 @@ HZ_API int hz_matvec_pair(hz_operator *op, int precision, const double *p_re, co
 HZ_API int hz_matvec_multi(hz_operator *op, int precision, int nrhs, const double *p_re,
                     const double *p_im, double *q_re, double *q_im, int where);
 
-/* Solve A X = B for nrhs right-hand sides ([nrhs][n] each) with BiCGSTAB in
- * lockstep over the columns, every product a multi right-hand-side sweep;
- * HZ_PREC_F32_REFINED refines every column with FP64 residuals.  resid (may
- * be NULL) receives each column's final relative residual. */
+/* Solve A X = B for nrhs right-hand sides ([nrhs][n] each) in lockstep over
+ * the columns, every product a multi right-hand-side sweep over the columns
+ * still iterating: opts->method HZ_GMRES runs one GMRES(restart) per column
+ * (basis of (restart + 3) x nrhs x n complex FP64 vectors), any other method
+ * BiCGSTAB.  HZ_PREC_F32_REFINED refines every column with FP64 residuals.
+ * resid (may be NULL) receives each column's final relative residual. */
 HZ_API int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts, int nrhs, const double *b_re,
                           const double *b_im, double *x_re, double *x_im, int where,
                           hz_solve_info *info, double *resid);

@@ -7,8 +7,9 @@ against this library's single-vector path.
 * every operator of an uneven batch (one persistent launch over four
   ellipsoids with different grids and wave numbers) against the oracle's
   product on that operator's own tube: 1e-12 (FP64), 2e-5 (FP32);
-* a lockstep multi-RHS FP32 + FP64-refinement solve of five plane waves to
-  1e-11 against the oracle's BiCG solve of each wave to 1e-13: 1e-8.
+* lockstep multi-RHS solves of five plane waves (BiCGSTAB and GMRES, FP32 +
+  FP64 refinement to 1e-11, and plain FP64 GMRES to 1e-12) against the
+  oracle's BiCG solve of each wave to 1e-13: 1e-8.
 """
 import numpy as np
 import pytest
@@ -44,12 +45,15 @@ def test_multi_rhs_columns_vs_oracle(hz, oracle):
         # lockstep refined solve of plane waves against the oracle's solves
         dirs = G.fibonacci_sphere(5)
         B = op.rhs_plane_waves(dirs)
-        X, info, res = op.solve_multi(B, method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=1e-11,
-                                      inner_tol=1e-5)
-        assert np.all(res < 1e-11)
-        for r in range(B.shape[0]):
-            xo, it, ro = oracle.bicg(po, tp, B[r], acc=1e-13)
-            assert rel_err(X[r], xo) < 1e-8, r
+        xos = [oracle.bicg(po, tp, B[r], acc=1e-13)[0] for r in range(B.shape[0])]
+        runs = [dict(method=hz.BICGSTAB, precision=hz.PREC_F32_REFINED, tol=1e-11, inner_tol=1e-5),
+                dict(method=hz.GMRES, precision=hz.PREC_F32_REFINED, tol=1e-11, inner_tol=1e-5, restart=40),
+                dict(method=hz.GMRES, precision=hz.PREC_F64, tol=1e-12, restart=30)]
+        for kw in runs:
+            X, info, res = op.solve_multi(B, **kw)
+            assert np.all(res < kw["tol"]), (kw, res)
+            for r in range(B.shape[0]):
+                assert rel_err(X[r], xos[r]) < 1e-8, (kw, r)
 
 
 def test_batch_products_vs_oracle(hz, oracle):
