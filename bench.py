@@ -654,7 +654,7 @@ def run_plane_waves(a):
                                       restart=a.restart)
         out["multi_solve"] = dict(info, max_resid=float(np.max(res)), method=a.multi_method)
         nsingle = min(R, a.single_waves)
-        for meth, name in ((hz.BICGSTAB, "bicgstab"), (hz.GMRES, "gmres")):
+        for meth, name in ((hz.BICGSTAB, "bicgstab"), (hz.GMRES, "gmres")) if nsingle > 0 else ():
             t0 = time.perf_counter()
             errs = []
             for r in range(nsingle):
