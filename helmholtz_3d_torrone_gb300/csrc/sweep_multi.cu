@@ -10,7 +10,6 @@
 // cross-tile sums, with no FP64 instruction in its tile loop); the
 // densities of a tile are staged as RB/2 rows of two complex values each.
 #include "hz_internal.cuh"
-#include "sincos64.cuh"
 #include "pair64.cuh"
 #include "bulk_copy.cuh"
 #include "krylov_multi.cuh"
