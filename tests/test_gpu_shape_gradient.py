@@ -12,10 +12,14 @@ J is only piecewise smooth: a tiny move of phi can carry a pair across the
 near-field radius tau (regularised value against kernel value) or flip an
 upwind / limiter branch of the stencils, and then a difference quotient
 measures the jump, not a derivative.  So a node is used only where the
-quotients with steps 1e-6 and 1e-7 agree to 1e-3 (at least 6 of 12 seeded
-candidates); there the GPU gradient matches the 1e-7 quotient to 2e-3 of
-the largest checked component.  Nodes within 0.5 h of the tube boundary
+quotients with steps 1e-6 and 2e-6 agree to 1e-5 of the largest quotient
+(at least 6 of 12 seeded candidates); there the GPU gradient matches the
+step-1e-6 quotient to 1e-6 of the largest one on at least 5 nodes and to
+1e-4 on all (a branch within a step of a node bends both quotients alike
+and passes the screen).  Nodes within 0.5 h of the tube boundary
 |phi| = eps are not candidates (membership changes are not differentiated).
+tests/test_gpu_grad_vs_reference.py makes the same check against the
+reference build's own solves.
 """
 import numpy as np
 import pytest
@@ -68,15 +72,13 @@ def test_shape_gradient_vs_oracle_finite_differences(hz, oracle):
         dm[q] -= h
         return (oracle_J(oracle, dp, rx, t) - oracle_J(oracle, dm, rx, t)) / (2 * h)
 
-    smooth, ref = [], []
-    for q in nodes:
-        a, b = fd(q, 1e-6), fd(q, 1e-7)
-        if abs(a - b) <= 1e-3 * abs(b):
-            smooth.append(q)
-            ref.append(b)
-    assert len(smooth) >= 6, len(smooth)
-    ref = np.array(ref)
-    gq = np.array([g[q] for q in smooth])
-    scale = np.max(np.abs(ref))
+    q1 = np.array([fd(q, 1e-6) for q in nodes])
+    q2 = np.array([fd(q, 2e-6) for q in nodes])
+    scale = np.max(np.abs(q1))
     assert scale > 0
-    assert np.max(np.abs(gq - ref)) <= 2e-3 * scale, (gq, ref)
+    smooth = np.abs(q1 - q2) <= 1e-5 * scale
+    assert np.count_nonzero(smooth) >= 6, (q1, q2)
+    gq = np.array([g[q] for q in nodes])
+    err = np.abs(gq - q1)[smooth] / scale
+    assert np.count_nonzero(err <= 1e-6) >= 5, (err, gq[smooth], q1[smooth])
+    assert np.max(err) <= 1e-4, (err, gq[smooth], q1[smooth])
