@@ -100,6 +100,8 @@ def parse():
     ap.add_argument("--method", choices=["bicg", "gmres"], nargs="*", default=["bicg", "gmres"],
                     help="--solve: inner Krylov method(s) of the refined solves")
     ap.add_argument("--restart", type=int, default=40, help="--solve: GMRES restart length")
+    ap.add_argument("--phase", choices=["direct", "split"], default="direct",
+                    help="--solve: phase mode of the FP32 sweeps (hz_set_phase_mode)")
     ap.add_argument("--inner-tol", type=float, default=INNER_TOL,
                     help="--solve: tightest inner FP32 tolerance of the refined solves")
     ap.add_argument("--save", default="",
@@ -535,6 +537,10 @@ def run_solve(a, local):
                                          "Dirichlet point source at (0.1,0.05,0)" % (a.reinit_iters, N, wave))
             out["config"]["reinit_max_err_in_band"] = reinit_err
         out["config"]["sweep_variant"] = op.autotune()[0]
+        if a.phase == "split":
+            op.set_phase_mode(hz.PHASE_SPLIT)
+        out["config"]["phase"] = a.phase
+        out["config"]["inner_tol_floor"] = a.inner_tol
         b = op.rhs_point_source(src, hz.RHS_POINT_DIRICHLET)
         sols = {}
         for meth in a.method:
