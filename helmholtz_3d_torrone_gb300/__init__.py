@@ -330,7 +330,7 @@ class Operator:
         _check(load().hz_set_sweep_config(self.h, cfg))
 
     def set_phase_mode(self, mode):
-        """PHASE_DIRECT (default) or PHASE_SPLIT for the FP32 pair sweep."""
+        """PHASE_SPLIT (default) or PHASE_DIRECT for the FP32 pair sweep."""
         _check(load().hz_set_phase_mode(self.h, mode))
 
     def sweep_timing(self, enable=-1):

@@ -283,7 +283,7 @@ struct hz_operator {
     hz::SweepTimer timer;
     int sweep_cfg = 0;  // FP32 sweep variant of the fused A p + A^H pt pass (hz_autotune)
     int sweep_cfg_a = -1;  // variant of the single-product passes (A p or A^H p); -1: sweep_cfg
-    int phase_mode = 0; // HZ_PHASE_DIRECT or HZ_PHASE_SPLIT (hz_set_phase_mode)
+    int phase_mode = HZ_PHASE_SPLIT; // HZ_PHASE_SPLIT (default) or HZ_PHASE_DIRECT (hz_set_phase_mode)
     // Combo formulation (hz_set_combo): annulus points, FP64 products only
     int combo = 0;
     hz_dense_opts combo_opts{};

@@ -53,9 +53,9 @@ extern "C" {
 
 /* Arithmetic of a matvec or solve. */
 #define HZ_PREC_F64 0         /* plain FP64 everywhere                                  */
-#define HZ_PREC_F32 1         /* FP32 pair sweep (tile-local origins; phase k rho passed
-                                 to the SFU sin/cos, or split-k with hz_set_phase_mode),
-                                 FP64 inner products                                    */
+#define HZ_PREC_F32 1         /* FP32 pair sweep (tile-local origins; phase k rho reduced
+                                 with a split k/(2 pi), or passed straight to the SFU
+                                 sin/cos: hz_set_phase_mode), FP64 inner products        */
 #define HZ_PREC_F32_REFINED 2 /* FP32 inner solves inside FP64 iterative refinement whose
                                  residual b - A x uses the FP64 sweep                   */
 
@@ -174,12 +174,14 @@ HZ_API int hz_autotune(hz_operator *op, int *chosen, double *ms_per_sweep);
 HZ_API int hz_set_sweep_config(hz_operator *op, int cfg);
 
 /* Phase of the FP32 pair sweep (hz_matvec, hz_matvec_pair and the FP32
- * products of hz_solve).  HZ_PHASE_DIRECT (default): k rho goes to the SFU's
- * sin/cos as one FP32 product.  HZ_PHASE_SPLIT: the phase is first reduced in
- * revolutions with k/(2 pi) split into an FP32 head and tail, which about
- * halves the FP32-vs-FP64 product error (e.g. 4.5e-8 -> 2.9e-8 on a 256^3
- * torus at k = 20) at about 6 % of the sweep's throughput.  The multi
- * right-hand-side, batch and Combo FP32 sweeps use the direct phase. */
+ * products of hz_solve).  HZ_PHASE_SPLIT (default): the phase is first
+ * reduced in revolutions with k/(2 pi) split into an FP32 head and tail,
+ * which about halves the FP32-vs-FP64 product error (4.6e-8 -> 2.9e-8 on the
+ * 256^3 torus at k = 20) at about 6 % of the sweep's throughput; there a
+ * refined solve to 1e-6 then needs one FP64 residual instead of two (55 s
+ * instead of 84 s).  HZ_PHASE_DIRECT: k rho goes to the SFU's sin/cos as one
+ * FP32 product.  The multi right-hand-side, batch and Combo FP32 sweeps use
+ * the direct phase. */
 #define HZ_PHASE_DIRECT 0
 #define HZ_PHASE_SPLIT 1
 HZ_API int hz_set_phase_mode(hz_operator *op, int mode);

@@ -102,7 +102,7 @@ def _product_errors(hz, op, seed):
         q32 = op.matvec(v, precision=hz.PREC_F32)
         out[name] = float(np.linalg.norm(q32 - q64) / np.linalg.norm(q64))
         out[name + "_max"] = float(np.max(np.abs(q32 - q64)) / np.max(np.abs(q64)))
-    op.set_phase_mode(hz.PHASE_DIRECT)
+    op.set_phase_mode(hz.PHASE_SPLIT)  # back to the default
     return out
 
 
