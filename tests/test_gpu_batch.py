@@ -2,8 +2,9 @@
 different grids and wave numbers.
 
 * FP32 batched product (one persistent launch over all operators) equals
-  each operator's own FP32 product to 1e-10 (same tiles; only the grouping
-  of cross-tile sums differs) for every batch sweep shape;
+  each operator's own FP32 product with the direct phase (the batch sweep's)
+  to 1e-10 (same tiles; only the grouping of cross-tile sums differs) for
+  every batch sweep shape;
 * FP64 batched product equals each operator's FP64 product bit for bit;
 * the batched FP32 + FP64-refinement BiCGSTAB solve equals each operator's
   FP64 solve to 1e-8 (both to 1e-11).
@@ -45,7 +46,13 @@ def test_batch_products(hz, batch):
     q64 = b.matvec(vs, precision=hz.PREC_F64)
     for op, v, q in zip(ops, vs, q64):
         assert np.array_equal(q, op.matvec(v, precision=hz.PREC_F64))
+    # the batch sweep reduces the phase directly (HZ_PHASE_DIRECT); compare
+    # with each operator's own FP32 product in that mode
+    for op in ops:
+        op.set_phase_mode(hz.PHASE_DIRECT)
     ref32 = [op.matvec(v, precision=hz.PREC_F32) for op, v in zip(ops, vs)]
+    for op in ops:
+        op.set_phase_mode(hz.PHASE_SPLIT)
     for shape in range(4):
         b.set_variant(shape)
         q32 = b.matvec(vs, precision=hz.PREC_F32)
