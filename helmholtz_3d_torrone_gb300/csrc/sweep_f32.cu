@@ -10,14 +10,14 @@
 //    x_t - o = (t_hi - o_hi) + (t_lo - o_lo): the head difference is rounded
 //    to half an ulp of itself, so the offset of close pairs keeps FP32
 //    relative precision with no FP64 instruction in the tile loop.
-//  * The phase k*rho goes to the SFU's sin/cos as one FP32 product: rho
-//    itself carries an FP32 rounding, so the phase error is a few 1e-7
-//    rad times k rho either way.  The FP32 product then stays within
-//    1e-7 of the FP64 product (4.5e-8 on the 256^3 torus at k = 20,
-//    3.3e-7 on 128^3 at k = 40), far below the 1e-5 inner tolerance.
-//    Reducing the phase in revolutions with a split k/(2 pi) first
-//    (hz_set_phase_mode(op, HZ_PHASE_SPLIT), the MODE bit
-//    SWEEP_PHASE_SPLIT) halves that error at 6 % of the throughput.
+//  * The phase k*rho is reduced in revolutions with k/(2 pi) split into an
+//    FP32 head and tail before the SFU's sin/cos (the MODE bit
+//    SWEEP_PHASE_SPLIT, the operator's default), or passed to the SFU as one
+//    FP32 product (hz_set_phase_mode(op, HZ_PHASE_DIRECT)).  rho itself
+//    carries an FP32 rounding, so some phase error remains either way; the
+//    FP32 product stays within 1e-7 of the FP64 product (2.9e-8 split,
+//    4.6e-8 direct on the 256^3 torus at k = 20), and the split reduction
+//    costs about 6 % of the throughput.
 //  * The near-field test rho <= tau is decided in FP64 (with the FP64
 //    sweep's own arithmetic) whenever the FP32 rho^2 lies within 1e-4 of
 //    tau^2, so FP32 and FP64 operators classify every pair alike.
