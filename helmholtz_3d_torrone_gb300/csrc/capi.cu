@@ -912,6 +912,20 @@ int hz_solve_multi(hz_operator *op, const hz_solve_opts *opts_in, int nrhs, cons
     }
     const bool gm = o.method == HZ_GMRES;
     HZ_CHECK_CUDA(cudaSetDevice(op->device));
+    if (gm) {
+        // the lockstep GMRES basis is (restart + 3) x nrhs x n complex
+        // doubles: say so plainly when it cannot fit
+        const size_t need = gmres_multi_work_bytes(op->n, nrhs, o.restart);
+        size_t free_b = 0, total_b = 0;
+        HZ_CHECK_CUDA(cudaMemGetInfo(&free_b, &total_b));
+        const size_t have = op->solver->mgwork.bytes;
+        if (need > have && need - have > free_b) {
+            set_error("hz_solve_multi: the GMRES basis for %d columns and restart %d needs %.1f GB, %.1f GB free "
+                      "(lower restart or solve fewer columns per call)",
+                      nrhs, o.restart, need / 1e9, (free_b + have) / 1e9);
+            return HZ_ERR_ARG;
+        }
+    }
     cudaStream_t s = op->stream;
     hz_solver_state *st = op->solver;
     const int64_t n = op->n;
