@@ -136,6 +136,11 @@ def parse():
                     help="instead of the step benchmark: build the torus operator at --N and run --steps products of "
                          "this kind (A p, or the fused A p + A^H pt), timed with CUDA events (short runs for "
                          "profilers)")
+    ap.add_argument("--config1", action="store_true",
+                    help="instead of the step benchmark: the 64^3 sphere (k = 5, point source at the origin) solved "
+                         "to 1e-13 on the GPU (FP64 BiCG and FP32 + FP64-refinement GMRES) and by the reference "
+                         "build on the host cores (its dense matrix and CompBiCG), end to end, with the densities "
+                         "compared")
     ap.add_argument("--sweep-variant", type=int, default=-1,
                     help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
@@ -903,6 +908,65 @@ def run_batch(a):
     return 0
 
 
+def run_config1(a):
+    """Configuration 1 end to end on both sides: the GPU library (build,
+    FP64 BiCG and refined GMRES solves to 1e-13) and the reference build on
+    the host cores (grids, tube, per-point set-up and its dense matrix, then
+    CompBiCG to 1e-13; oracle/ref_worker.py, timed as the CPU baseline)."""
+    import numpy as np
+    import helmholtz_3d_torrone_gb300 as hz
+    from helmholtz_3d_torrone_gb300 import geometry as G
+    from oracle.ref_worker import RefWorker
+    N, k = 64, 5.0
+    d = G.sphere(N, radius=0.5)
+    out = {"mode": "config1", "config": {"workload": "sphere R=0.5 at the origin, exact signed distance on 64^3 over "
+                                                     "[-1,1]^3, tube |phi|<=3h, k=5, Dirichlet point source at the "
+                                                     "origin, solves to relative residual 1e-13", "N": N, "wave": k}}
+    rx = G.random_sphere_points(100, 0.9, seed=2024)
+    r = np.linalg.norm(rx, axis=1)
+    ue = np.exp(1j * k * r) / (4 * np.pi * r)
+    t0 = time.perf_counter()
+    op = hz.Operator(hz.params(N, k, int_l=-1.0, int_u=1.0, factor=3.0, tau_factor=2.0, dirichlet=1))
+    op.set_distance(d)
+    n = op.build()
+    t_build = time.perf_counter() - t0
+    b = op.rhs_point_source(np.zeros(3), hz.RHS_POINT_DIRICHLET)
+    op.solve(b, method=hz.GMRES, precision=hz.PREC_F32_REFINED, tol=1e-6, restart=120)  # loads the kernels
+    gpu = {"n_tube": n, "build_s": t_build}
+    xs = {}
+    for name, kw in (("f64_bicg", dict(method=hz.BICG, precision=hz.PREC_F64, tol=1e-13, maxit=1000)),
+                     ("refined_gmres", dict(method=hz.GMRES, precision=hz.PREC_F32_REFINED, tol=1e-13,
+                                            restart=120))):
+        t1 = time.perf_counter()
+        x, info = op.solve(b, **kw)
+        dt = time.perf_counter() - t1
+        u = op.evaluate(rx, x, hz.DOUBLE_LAYER)
+        xs[name] = x
+        gpu[name] = {"seconds": dt, "iterations": info["iterations"], "resid": info["resid"],
+                     "field_rel_err_vs_exact": float(np.max(np.abs(u - ue)) / np.max(np.abs(ue)))}
+    op.close()
+    t2 = time.perf_counter()
+    with RefWorker("dirichlet", N, k, d) as ref:
+        t_setup = time.perf_counter() - t2
+        t3 = time.perf_counter()
+        xr = ref.solve(b)
+        t_solve = time.perf_counter() - t3
+    cpu = {"setup_and_dense_s": t_setup, "compbicg_s": t_solve, "total_s": t_setup + t_solve,
+           "cores": os.cpu_count(), "kind": "reference",
+           "what": "reference build: ASSIGN_GRADIENT, BothCurvs loop, tube, per-point set-up and the dense matrix "
+                   "of omp_get_Ccomp entries (OpenMP), then CompBiCG to 1e-13 (DEFAULTACC of this build)"}
+    for name, x in xs.items():
+        gpu[name]["density_rel_err_vs_reference"] = float(np.max(np.abs(x - xr)) / np.max(np.abs(xr)))
+    gpu_total = t_build + gpu["refined_gmres"]["seconds"]
+    out.update(gpu=gpu, cpu_reference=cpu,
+               speedup_end_to_end=cpu["total_s"] / gpu_total,
+               note="GPU end to end = build + refined GMRES solve (kernels loaded beforehand); the reference's "
+                    "end to end = its set-up with the dense matrix + CompBiCG, in a child process")
+    print(json.dumps(out))
+    sys.stdout.flush()
+    return 0
+
+
 def run_product(a):
     """--steps products of one kind on the torus at --N (after --warmup)."""
     import numpy as np
@@ -942,6 +1006,12 @@ def main():
     rank, world, local = dist_env()
     if a.impl == "reference":
         return run_reference(a, rank, world)
+    if a.config1:
+        # the reference worker's child processes start with spawn, which is
+        # safe after this process has initialised CUDA
+        import torch
+        torch.cuda.set_device(local)
+        return run_config1(a)
     if a.solve or a.plane_waves or a.batch or a.gradient or a.combo or a.product:
         import torch
         torch.cuda.set_device(local)
