@@ -946,7 +946,7 @@ def run_config1(a):
                      "field_rel_err_vs_exact": float(np.max(np.abs(u - ue)) / np.max(np.abs(ue)))}
     op.close()
     t2 = time.perf_counter()
-    with RefWorker("dirichlet", N, k, d) as ref:
+    with RefWorker("dirichlet", N, k, d, omp_chunk=16) as ref:
         t_setup = time.perf_counter() - t2
         t3 = time.perf_counter()
         xr = ref.solve(b)
@@ -954,7 +954,8 @@ def run_config1(a):
     cpu = {"setup_and_dense_s": t_setup, "compbicg_s": t_solve, "total_s": t_setup + t_solve,
            "cores": os.cpu_count(), "kind": "reference",
            "what": "reference build: ASSIGN_GRADIENT, BothCurvs loop, tube, per-point set-up and the dense matrix "
-                   "of omp_get_Ccomp entries (OpenMP), then CompBiCG to 1e-13 (DEFAULTACC of this build)"}
+                   "of omp_get_Ccomp entries (OpenMP), then omp_CompBiCG (OpenMP, chunk 16 as the driver's "
+                   "DEFAULT_OMP_CACHE_CHUNKSIZE) to 1e-13 (DEFAULTACC of this build)"}
     for name, x in xs.items():
         gpu[name]["density_rel_err_vs_reference"] = float(np.max(np.abs(x - xr)) / np.max(np.abs(xr)))
     gpu_total = t_build + gpu["refined_gmres"]["seconds"]

@@ -276,7 +276,7 @@ class Reference:
         L.ref_tube_points.restype = C.c_int
         L.ref_entries.argtypes = [C.c_int, C.c_int64, _i32p, _i32p, _dp, _dp]
         L.ref_dense_rows.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, C.c_int]
-        L.ref_compbicg.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp]
+        L.ref_compbicg.argtypes = [C.c_int, _dp, _dp, _dp, _dp, _dp, _dp, C.c_int]
         L.ref_rows_matvec.argtypes = [C.c_int, C.c_int, C.c_int, _dp, _dp, _dp, _dp, C.c_int]
         L.ref_double_layer.argtypes = [C.c_int, C.c_double, _dp, _dp, _dp]
         L.ref_combo.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double] + [_dp] * 5
@@ -384,11 +384,12 @@ class Reference:
         self.L.ref_rows_matvec(n, r0, r1, _d(vr), _d(vi), _d(qr), _d(qi), nthreads)
         return qr + 1j * qi
 
-    def compbicg(self, are, aim, b):
+    def compbicg(self, are, aim, b, chunk=0):
+        """The reference's CompBiCG (chunk <= 0) or omp_CompBiCG (chunk > 0)."""
         n = are.shape[0]
         br = np.ascontiguousarray(b.real)
         bi = np.ascontiguousarray(b.imag)
         xr, xi = np.empty(n), np.empty(n)
         self.L.ref_compbicg(n, _d(np.ascontiguousarray(are)), _d(np.ascontiguousarray(aim)), _d(br), _d(bi),
-                            _d(xr), _d(xi))
+                            _d(xr), _d(xi), int(chunk))
         return xr + 1j * xi

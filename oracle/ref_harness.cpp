@@ -41,6 +41,8 @@ double cal_delta(double epsilon, double x);
 double omp_get_Ccomp(int size, int pi, int pj, double epsilon, double tempC[]);
 int CompBiCG(int size, double *density, double *densityimg, double **Kernel, double **Kernelimg,
              double *b, double *bimg);
+int omp_CompBiCG(int size, double *density, double *densityimg, double **Kernel, double **Kernelimg,
+                 double *b, double *bimg, int chunk);
 int DoubleLayerKernel(int size, double epsilon, double ***level, double ***leveldx, double ***leveldy,
                       double ***leveldz, double ***levelmcurv, double ***levelgcurv, double *zxlist, double *zylist,
                       double *zzlist, double *zxstarlist, double *zystarlist, double *zzstarlist, double *dist,
@@ -338,8 +340,11 @@ void ref_sphere(double *out)
 }
 
 /* CompBiCG (BICGSTAB.c:5-339) on a row-major dense matrix. */
+// chunk <= 0: the serial CompBiCG (BICGSTAB.c:5); chunk > 0: the OpenMP
+// omp_CompBiCG (BICGSTAB.c:344) with that schedule chunk (the driver's
+// DEFAULT_OMP_CACHE_CHUNKSIZE is 16, large3Dexample2.c:38).
 int ref_compbicg(int n, const double *are, const double *aim, const double *b, const double *bimg,
-                 double *x, double *ximg)
+                 double *x, double *ximg, int chunk)
 {
     double **K = (double **)malloc(n * sizeof(double *));
     double **Ki = (double **)malloc(n * sizeof(double *));
@@ -352,7 +357,7 @@ int ref_compbicg(int n, const double *are, const double *aim, const double *b, c
     double *bb = (double *)malloc(n * sizeof(double)), *bi = (double *)malloc(n * sizeof(double));
     memcpy(bb, b, n * sizeof(double));
     memcpy(bi, bimg, n * sizeof(double));
-    int rc = CompBiCG(n, x, ximg, K, Ki, bb, bi);
+    int rc = (chunk > 0) ? omp_CompBiCG(n, x, ximg, K, Ki, bb, bi, chunk) : CompBiCG(n, x, ximg, K, Ki, bb, bi);
     for (int i = 0; i < n; i++) {
         free(K[i]);
         free(Ki[i]);

@@ -17,7 +17,7 @@ import os
 import numpy as np
 
 
-def _serve(conn, variant, N, wave, d, want_matrix, threads):
+def _serve(conn, variant, N, wave, d, want_matrix, threads, chunk):
     os.environ["OMP_NUM_THREADS"] = str(threads)
     import oracle as O
     devnull = os.open(os.devnull, os.O_WRONLY)
@@ -36,22 +36,23 @@ def _serve(conn, variant, N, wave, d, want_matrix, threads):
         msg = conn.recv()
         if msg is None:
             break
-        conn.send(ref.compbicg(are, aim, msg))
+        conn.send(ref.compbicg(are, aim, msg, chunk))
     conn.close()
 
 
 class RefWorker:
     """One reference configuration in a child process: .tube has the
     reference's tube (idx, xs, nrm, delta, jac, reg, w, and the dense matrix
-    as A with matrix=True); .solve(b) runs CompBiCG on it."""
+    as A with matrix=True); .solve(b) runs CompBiCG on it (omp_CompBiCG with
+    that OpenMP chunk when omp_chunk > 0)."""
 
-    def __init__(self, variant, N, wave, d, matrix=False, timeout=900, threads=None):
+    def __init__(self, variant, N, wave, d, matrix=False, timeout=900, threads=None, omp_chunk=0):
         ctx = mp.get_context("spawn")
         self.timeout = timeout
         threads = threads or (os.cpu_count() or 1)
         self.conn, child = ctx.Pipe()
         self.proc = ctx.Process(target=_serve, args=(child, variant, N, wave, np.ascontiguousarray(d), matrix,
-                                                     threads), daemon=True)
+                                                     threads, omp_chunk), daemon=True)
         self.proc.start()
         child.close()
         self.tube = self._recv()
