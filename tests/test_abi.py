@@ -102,6 +102,7 @@ def test_null_handles_and_bad_arguments(hz):
         "hz_batch_create": lambda: L.hz_batch_create(None, 0, C.byref(C.c_void_p())),
         "hz_batch_solve": lambda: L.hz_batch_solve(None, C.byref(opts), None, None, None, None, hz.HZ_HOST,
                                                    C.byref(info), None),
+        "hz_residual_history": lambda: L.hz_residual_history(None, None, 0, C.byref(C.c_int())),
     }
     for name, call in cases.items():
         rc = call()
