@@ -60,6 +60,13 @@ RESTART = 120        # GMRES basis size (no restart within these solves)
 #          --fp64-full --fp64-tol 1e-6 --fp64-method gmres
 # (1,708 s, FP64 residual 8.4e-7).
 FP64_SOLVE_ITERS = 67
+FP64_SOLVE_ITERS_WORKLOAD = (256, 20.0)  # (N, k) the count was measured on
+
+
+def fp64_solve_products(N, wave):
+    """The measured FP64 product count, for the workload it was measured on
+    only (None for any other --N / --wave)."""
+    return FP64_SOLVE_ITERS if (N, float(wave)) == FP64_SOLVE_ITERS_WORKLOAD else None
 # DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
 # 22.36 MB measured by ncu on the 128^3 torus (n = 145,272), scaled by n to
 # n = 581,420.  The sweep reads every record once from DRAM and the tiles
@@ -183,13 +190,15 @@ def solve_desc():
                     "flushed between steps by a 256 MB device write; the steps give the FP32 pair rate"}
 
 
-def cpu_solve_seconds(pair_rate, n):
+def cpu_solve_seconds(pair_rate, n, N=256, wave=20.0):
     """Lower bound of the reference's FP64 solve time on the host cores:
-    FP64_SOLVE_ITERS products x n^2 pair evaluations / the measured rate
-    (its BiCG evaluates two products per iteration)."""
-    if not FP64_SOLVE_ITERS or not pair_rate:
+    the measured FP64 product count x n^2 pair evaluations / the measured
+    rate (its BiCG evaluates two products per iteration); None where no
+    count was measured."""
+    prods = fp64_solve_products(N, wave)
+    if not prods or not pair_rate:
         return None
-    return FP64_SOLVE_ITERS * 1.0 * n * n / pair_rate
+    return prods * 1.0 * n * n / pair_rate
 
 
 def cpu_rate(N, wave, impl, steps, warmup, step_seconds, timeout=900):
@@ -262,7 +271,7 @@ def run_reference(a, rank, world):
     total_s = sum(r["seconds_per_step"])
     rate = total_pairs / total_s
     n = r["n"]
-    solve_s = cpu_solve_seconds(rate, n)
+    solve_s = cpu_solve_seconds(rate, n, a.N, a.wave)
     kind = "reference" if r["impl"] == "reference" else "port"
     sample = ("%d target rows x %d sources per step (one row block of an A p product, the reference's pair "
               "evaluation + complex MAC), %d steps after %d warm-up; setup %.1f s untimed"
@@ -274,7 +283,8 @@ def run_reference(a, rank, world):
         "config": dict(workload_desc(a.N, a.wave, n), tol=SOLVE_TOL, method="FP64 (the reference's pair formula)",
                        value="lower bound of the FP64 solve time on the host cores: %s products (of the complete "
                              "FP64 GMRES(%d) GPU solve of this workload; the reference's BiCG needs two per "
-                             "iteration) x n^2 pairs / the measured pair rate" % (FP64_SOLVE_ITERS, RESTART),
+                             "iteration) x n^2 pairs / the measured pair rate"
+                             % (fp64_solve_products(a.N, a.wave), RESTART),
                        step="reference pair evaluation + complex MAC over a bounded block of target rows x all n "
                             "sources"),
         "pair_rate_gpair_s": rate / 1e9,
@@ -428,8 +438,9 @@ def run_gb300(a, rank, world, local):
         per_prod = ev4.elapsed_time(ev5) / 1e3 / a.fp64_iters
         f64 = {"seconds_per_product": per_prod, "products_timed": a.fp64_iters,
                "gpair_per_s": float(n) * n / per_prod / 1e9,
-               "solve_products": FP64_SOLVE_ITERS,
-               "solve_s_extrapolated": per_prod * FP64_SOLVE_ITERS if FP64_SOLVE_ITERS else None,
+               "solve_products": fp64_solve_products(N, wave),
+               "solve_s_extrapolated": (per_prod * fp64_solve_products(N, wave)
+                                        if fp64_solve_products(N, wave) else None),
                "how": "measured seconds of one FP64 product (sweep64_kernel, CUDA events) x the product count of "
                       "a complete FP64 GMRES(%d) solve of this workload to the same tol, measured once (bench.py "
                       "--solve --fp64-full); GMRES adds only FP64 Gram-Schmidt (milliseconds) per product" % RESTART}
@@ -496,7 +507,7 @@ def run_gb300(a, rank, world, local):
         try:
             r = cpu_rate(N, wave, "auto", 2, 1, a.cpu_seconds)
             rate = sum(r["pairs_per_s"]) / len(r["pairs_per_s"])
-            cs = cpu_solve_seconds(rate, n)
+            cs = cpu_solve_seconds(rate, n, N, wave)
             line["cpu_baseline"] = {"value": cs, "unit": "s", "cores": r["threads"],
                                     "kind": "reference" if r["impl"] == "reference" else "port",
                                     "pair_rate_gpair_s": rate / 1e9,
@@ -504,7 +515,7 @@ def run_gb300(a, rank, world, local):
                                               "warm-up, same 256^3 torus operator; setup %.1f s untimed; value = "
                                               "lower bound of the reference's FP64 solve (%s products x n^2 / rate)"
                                               % (r["rows"], r["n"], r["pairs_per_step"], r["setup_s"],
-                                                 FP64_SOLVE_ITERS)}
+                                                 fp64_solve_products(N, wave))}
         except Exception as e:  # report, do not hide the GPU number
             line["cpu_baseline"] = {"value": None, "unit": "s", "error": str(e)[:300]}
     print(json.dumps(line))
