@@ -67,6 +67,8 @@ def fp64_solve_products(N, wave):
     """The measured FP64 product count, for the workload it was measured on
     only (None for any other --N / --wave)."""
     return FP64_SOLVE_ITERS if (N, float(wave)) == FP64_SOLVE_ITERS_WORKLOAD else None
+
+
 # DRAM bytes (read + write) per launch of the fused FP32 sweep at 256^3:
 # 22.36 MB measured by ncu on the 128^3 torus (n = 145,272), scaled by n to
 # n = 581,420.  The sweep reads every record once from DRAM and the tiles
@@ -146,8 +148,8 @@ def parse():
     ap.add_argument("--config1", action="store_true",
                     help="instead of the step benchmark: the 64^3 sphere (k = 5, point source at the origin) solved "
                          "to 1e-13 on the GPU (FP64 BiCG and FP32 + FP64-refinement GMRES) and by the reference "
-                         "build on the host cores (its dense matrix and CompBiCG), end to end, with the densities "
-                         "compared")
+                         "build on the host cores (its dense matrix and omp_CompBiCG), end to end, with the "
+                         "densities compared")
     ap.add_argument("--sweep-variant", type=int, default=-1,
                     help="use this FP32 sweep variant instead of the autotuner's choice (profiling)")
     return ap.parse_args()
@@ -923,7 +925,8 @@ def run_config1(a):
     """Configuration 1 end to end on both sides: the GPU library (build,
     FP64 BiCG and refined GMRES solves to 1e-13) and the reference build on
     the host cores (grids, tube, per-point set-up and its dense matrix, then
-    CompBiCG to 1e-13; oracle/ref_worker.py, timed as the CPU baseline)."""
+    its OpenMP omp_CompBiCG to 1e-13; oracle/ref_worker.py, timed as the CPU
+    baseline)."""
     import numpy as np
     import helmholtz_3d_torrone_gb300 as hz
     from helmholtz_3d_torrone_gb300 import geometry as G
